@@ -1,0 +1,407 @@
+"""Throughput benchmark of the all-pairs normalised cross-correlation.
+
+One step = the whole hot path over one catalog already resident in HBM:
+kernel (a) (spectra + FP64 norms of every event/channel) then kernel (b)
+(every pair of the upper triangle: conj-products, inverse FFT, window
+max/min, normalisation, histograms, threshold, packed outputs).
+
+Default workload ("scale"): N=4096 events, 3 channels, L=2048 float32
+samples, lags -2047..2048 (shift 2048, padded size 4096), FP32 fused FFT
+form, seeded family-based synthetic waveforms.  Other workloads:
+--workload precision (N=16384, 1 channel, L=1024, +-128 lags) and
+--workload small (N=200, L=512, full lags).
+
+Prints ONE JSON line (rank 0).  With --impl reference the CPU path of the
+reference (its OpenMP source where it was built here, else the C
+restatement of it) is timed on the host cores on a bounded sample of the
+same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from seismic_gb300 import synth  # noqa: E402
+
+METRIC = "normalized xcorr pairs/sec at stated FP64-oracle error"
+WORKLOAD_TEXT = {
+    "scale": "N=4096 events x 3 channels x L=2048 float32, lags -2047..2048, padded FFT 4096, FP32 fused FFT form",
+    "precision": "N=16384 events x 1 channel x L=1024 float32, lags -127..128, padded FFT 2048, FP32 fused FFT form",
+    "small": "N=200 events x 1 channel x L=512 float32 (Ricker), lags -511..512, padded FFT 1024, FP32 fused FFT form",
+}
+CPU_SAMPLE_EVENTS = {"scale": 640, "precision": 1024, "small": 200}
+
+
+def fft_flops_per_pair(p: int, c: int) -> float:
+    """Algorithmic work per pair of the FFT form: one size-P inverse FFT
+    (2.5 P log2 P) plus C conj-products of P/2+1 bins (6 flops each)."""
+    return 2.5 * p * np.log2(p) + 6.0 * c * (p // 2 + 1)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", self.gpu_id], stdout=open(self.path, "w"),
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "power_w_max": float(max(power)),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------- FP64 check
+def fp64_sample_error(ev: np.ndarray, shift: int, p: int, vp, lp, vn, ln, n_sample: int = 2000, seed: int = 0):
+    """Max/mean |coef - FP64| and lag agreement on a random sample of pairs,
+    FP64 computed here with numpy (mean over channels of the per-channel
+    normalised circular correlation, lags 1-shift..shift, first maximum)."""
+    n = ev.shape[0]
+    rng = np.random.default_rng(seed)
+    i = rng.integers(0, n, n_sample)
+    j = rng.integers(0, n, n_sample)
+    i, j = np.minimum(i, j), np.maximum(i, j)
+    idx = i * n - i * (i - 1) // 2 + (j - i)
+    x = ev.astype(np.float64)
+    if x.ndim == 2:
+        x = x[:, None, :]
+    norms = np.sqrt((x * x).sum(-1))
+    inv = np.where(norms > 0, 1.0 / np.where(norms > 0, norms, 1), 0.0)
+    spec_i = np.fft.rfft(x[i], n=p, axis=-1) * inv[i][..., None]
+    spec_j = np.fft.rfft(x[j], n=p, axis=-1) * inv[j][..., None]
+    series = np.fft.irfft((spec_i * np.conj(spec_j)).mean(axis=1), n=p, axis=-1)
+    lags = np.arange(1 - shift, shift + 1)
+    s = series[:, np.mod(lags, p)]
+    amax, amin = s.argmax(1), s.argmin(1)
+    rvp = np.maximum(s.max(1), 0.0)
+    rvn = np.minimum(s.min(1), 0.0)
+    rlp = np.where(rvp > 0, lags[amax], 0)
+    rln = np.where(rvn < 0, lags[amin], 0)
+    top2 = np.partition(s, -2, axis=1)[:, -2:]
+    bot2 = np.partition(s, 1, axis=1)[:, :2]
+    gp, gn = top2[:, 1] - top2[:, 0], bot2[:, 1] - bot2[:, 0]
+    e = np.concatenate([np.abs(vp[idx] - rvp), np.abs(vn[idx] - rvn)])
+    mis = np.concatenate([(lp[idx] != rlp), (ln[idx] != rln)])
+    exempt = np.concatenate([gp < 1e-6, gn < 1e-6])
+    return {"max_abs": float(e.max()), "mean_abs": float(e.mean()),
+            "lag_agreement": float(1.0 - mis.mean()),
+            "lag_mismatch_not_exempt": int((mis & ~exempt).sum()), "pairs_sampled": int(n_sample)}
+
+
+# ----------------------------------------------------------- CPU baseline
+def cpu_baseline(workload: str, ev: np.ndarray, shift: int, n_sample: int | None = None, repeats: int = 1):
+    """The reference's CPU path on a bounded sample of the workload: its own
+    OpenMP source (built against the FFT shim) where available, else the C
+    restatement; one single-channel call per channel, all host cores."""
+    from oracle import oracle as O
+    n_s = n_sample or CPU_SAMPLE_EVENTS[workload]
+    sample = ev[:n_s]
+    cores = len(os.sched_getaffinity(0))
+    kind = "port"
+    fn = O.port_correlation_cpp
+    try:
+        if O.ref_lib() is not None:
+            kind, fn = "reference", O.ref_correlation_cpp
+    except OSError:
+        pass
+    p = 1 << int(sample.shape[-1]).bit_length()
+    c = sample.shape[1]
+    chans = [np.ascontiguousarray(sample[:, ch]) for ch in range(c)]
+    times = []
+    sys.stdout.flush()
+    saved = os.dup(1)
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)  # the reference's C code prints its parameters on stdout
+    try:
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            for x in chans:
+                fn(x, shift, 0.0, 20, num_threads=cores, chunk_size=4, padded=p)
+            times.append(time.perf_counter() - t0)
+    finally:
+        os.dup2(saved, 1)
+        os.close(saved)
+        os.close(devnull)
+    pairs = n_s * (n_s + 1) // 2
+    return {"value": pairs / float(np.median(times)), "unit": "pairs/s", "cores": cores, "kind": kind,
+            "sample": f"first {n_s} events of the same workload ({pairs} pairs x {c} channel(s), "
+                      f"one single-channel call per channel), median of {repeats}"}, times
+
+
+# --------------------------------------------------------------- the arms
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def run_reference(args):
+    ws, rank, _ = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return
+    ev, shift = synth.make_workload(args.workload, n_events=CPU_SAMPLE_EVENTS[args.workload])
+    for _ in range(args.warmup):
+        cpu_baseline(args.workload, ev, shift)
+    base, times = cpu_baseline(args.workload, ev, shift, repeats=args.steps)
+    n_s = CPU_SAMPLE_EVENTS[args.workload]
+    pairs = n_s * (n_s + 1) // 2
+    ms = float(np.mean(times)) * 1e3
+    out = {"metric": METRIC, "value": base["value"], "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "impl": "reference",
+           "data": "synthetic: seeded family-based waveforms (no public dataset; the reference's is not distributed)",
+           "config": {"workload": args.workload + ": " + WORKLOAD_TEXT[args.workload],
+                      "cpu_sample_events": n_s, "pairs_per_step": pairs},
+           "cpu_baseline": base, "e2e": {"value": base["value"], "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                                         "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def read_traffic(workload: str):
+    path = os.path.join(ROOT, "profiles", "pair_kernel_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        f = dict(kv.split("=", 1) for kv in line.split() if "=" in kv)
+        if f.get("workload") == workload and "dram_bytes_per_pair" in f:
+            return float(f["dram_bytes_per_pair"])
+    return None
+
+
+def run_ours(args):
+    import torch
+    from seismic_gb300 import _lib
+
+    ws, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.lib()
+    ev, shift = synth.make_workload(args.workload)
+    if ws > 1:  # weak scaling: every rank its own catalog of the same shape
+        ev = synth.family_catalog(ev.shape[0], ev.shape[1], ev.shape[2], seed=1000 + rank) \
+            if args.workload != "small" else ev
+    n, c, length = ev.shape
+    p = 1 << int(length).bit_length()
+    npairs = n * (n + 1) // 2
+    rows = n * c
+    prescale = 1 if c > 1 else 0
+
+    d_ev = torch.from_numpy(ev).to(dev)
+    spectra = torch.empty(rows * (p // 2) * 2, dtype=torch.float32, device=dev)
+    norms = torch.empty(rows, dtype=torch.float64, device=dev)
+    vp = torch.empty(npairs, dtype=torch.float32, device=dev)
+    lp = torch.empty(npairs, dtype=torch.int32, device=dev)
+    vn = torch.empty(npairs, dtype=torch.float32, device=dev)
+    ln = torch.empty(npairs, dtype=torch.int32, device=dev)
+    hist = torch.zeros(2, 20, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    stream = torch.cuda.Stream(dev)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+
+    def spectra_call():
+        _lib.check(lib.seismic_spectra_device(d_ev.data_ptr(), n, c, length, c * length, length, p, prescale,
+                                              spectra.data_ptr(), norms.data_ptr(), sh))
+
+    def pairs_call():
+        _lib.check(lib.seismic_pairs_device(spectra.data_ptr(), norms.data_ptr(), n, c, p, prescale, shift, 0.0, 20,
+                                            0, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(), ln.data_ptr(),
+                                            hist[0].data_ptr(), hist[1].data_ptr(), sh))
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            hist.zero_()
+            spectra_call()
+            pairs_call()
+    torch.cuda.synchronize(dev)
+
+    gpu_id = "0"
+    try:
+        props = torch.cuda.get_device_properties(dev)
+        gpu_id = f"{props.pci_domain_id:08x}:{props.pci_bus_id:02x}:{props.pci_device_id:02x}.0"
+    except Exception:
+        gpu_id = str(local)
+    clocks = ClockSampler(gpu_id)
+    ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    launches0 = lib.seismic_launch_count()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.zero_()                      # L2 flush between steps, outside the timed events
+            hist.zero_()
+            ev_s[3 * k].record(stream)
+            spectra_call()
+            ev_s[3 * k + 1].record(stream)
+            pairs_call()
+            ev_s[3 * k + 2].record(stream)
+    torch.cuda.synchronize(dev)
+    launches = lib.seismic_launch_count() - launches0
+    clk = clocks.stop()
+    t_spec = np.array([ev_s[3 * k].elapsed_time(ev_s[3 * k + 1]) for k in range(args.steps)]) * 1e-3
+    t_pair = np.array([ev_s[3 * k + 1].elapsed_time(ev_s[3 * k + 2]) for k in range(args.steps)]) * 1e-3
+    t_step = t_spec + t_pair
+    step_mean = float(t_step.mean())
+    if ws > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([step_mean], device=dev, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        step_mean = float(tt.item())
+    value = ws * npairs / step_mean
+
+    fp64 = fp64_sample_error(ev, shift, p, vp.cpu().numpy(), lp.cpu().numpy(), vn.cpu().numpy(),
+                             ln.cpu().numpy())
+
+    # ---- end-to-end through the public host entry point, pinned host buffers
+    e2e = None
+    if not args.skip_e2e:
+        h_ev = torch.empty(ev.shape, dtype=torch.float32, pin_memory=True)
+        h_ev.numpy()[...] = ev
+        h_out = [torch.empty(npairs, dtype=torch.float32 if k % 2 == 0 else torch.int32, pin_memory=True)
+                 for k in range(4)]
+        h_hist = [np.zeros(20, np.int32), np.zeros(20, np.int32)]
+
+        def host_call():
+            _lib.check(lib.seismic_xcorr_host(h_ev.data_ptr(), n, c, length, c * length, length, p, shift, 0.0, 20, 0,
+                                              *(t.data_ptr() for t in h_out), h_hist[0].ctypes.data,
+                                              h_hist[1].ctypes.data))
+        torch.cuda.set_device(dev)
+        host_call()
+        walls = []
+        for _ in range(max(3, min(args.steps, 10))):
+            t0 = time.perf_counter()
+            host_call()
+            walls.append(time.perf_counter() - t0)
+        e2e_t = float(np.mean(walls))
+        if ws > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_t = float(tt.item())
+        e2e = {"value": ws * npairs / e2e_t, "unit": "pairs/s", "h2d_bytes_per_step": int(ev.nbytes),
+               "d2h_bytes_per_step": int(4 * 4 * npairs + 2 * 20 * 4),
+               "entry_point": "seismic_xcorr_host (C ABI), pinned host buffers, wall clock per call"}
+
+    # ---- roofline of the dominant kernel (pair kernel: FP32 pipe)
+    flops = npairs * fft_flops_per_pair(p, c)
+    t_pair_mean = float(t_pair.mean())
+    achieved_tf = flops / t_pair_mean / 1e12
+    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+    sm_mhz = clk.get("sm_mhz") or 2070.0
+    peak_tf = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+    traffic_pp = read_traffic(args.workload)
+    roofline = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                "frac": achieved_tf / peak_tf,
+                "traffic": (traffic_pp * npairs) if traffic_pp is not None else None,
+                "kernel": "pair_kernel",
+                "peak_source": f"nominal FP32 FMA rate: {sm_count} SMs x 128 lanes x 2 flop x median SM clock "
+                               f"{sm_mhz:.0f} MHz under load (MEASURED_PEAKS.json has no FP32 figure)",
+                "work": f"{npairs} pairs x (2.5 P log2 P + 6 C (P/2+1)) flop, P={p}, C={c}",
+                "pair_kernel_ms": t_pair_mean * 1e3, "pair_kernel_share_of_step": t_pair_mean / step_mean}
+    spec_bytes = rows * (length * 4 + (p // 2) * 8 + 8)
+    spectra_roof = {"bound": "hbm", "achieved": spec_bytes / float(t_spec.mean()) / 1e9, "unit": "GB/s",
+                    "ms": float(t_spec.mean()) * 1e3, "bytes": int(spec_bytes)}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        spectra_roof["peak"] = peaks["hbm_gbs"]
+        spectra_roof["frac"] = spectra_roof["achieved"] / peaks["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        spectra_roof["peak"] = 6800.0
+        spectra_roof["peak_source"] = "fallback"
+
+    out = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": step_mean * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic: seeded family-based waveforms (no public dataset; the reference's is not distributed)",
+           "config": {"workload": args.workload + ": " + WORKLOAD_TEXT[args.workload], "n_events": n,
+                      "n_channels": c, "event_length": length, "shift": shift, "padded_size": p,
+                      "pairs_per_step": npairs, "form": "fp32",
+                      "l2": "L2 flushed (256 MB write) between timed steps; spectra > L2 for this workload"
+                      if rows * p * 4 > 129e6 else "L2 flushed (256 MB write) between timed steps"},
+           "fp64_error": fp64, "roofline": roofline, "spectra_kernel": spectra_roof, "e2e": e2e,
+           "clocks": clk, "gpu_launches": int(launches)}
+    if rank == 0 and not args.no_cpu_baseline:
+        base, _ = cpu_baseline(args.workload, ev, shift)
+        out["cpu_baseline"] = base
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOAD_TEXT), default="scale")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * seismic_gb300 -- C ABI of the GB300 (sm_103a) all-pairs normalised
+ * cross-correlation library (libseismic_gb300.so).
+ *
+ * Two groups of entry points:
+ *
+ *  1. Drop-in symbols with the exact names, argument lists and meaning of the
+ *     reference's ctypes boundary, so the reference's correlation_lib.py can
+ *     load this library instead of its own:
+ *       correlationCPP   Correlation_in_OMP/correlation_c.cpp:210-213
+ *                        (ctypes argtypes Correlation_in_OMP/correlation_lib.py:88-92)
+ *       correlationCUDA  Correlation_in_CUDA/correlation_cuda.cu:530-533
+ *                        (ctypes argtypes Correlation_in_CUDA/correlation_lib.py:77-80)
+ *       initialiseCUDA   Correlation_in_CUDA/correlation_cuda.cu:509
+ *                        (Correlation_in_CUDA/correlation_lib.py:101-106)
+ *     They return void like the originals; a failure is reported on stderr
+ *     and through seismic_last_error().  `events_reversed`, `num_threads` and
+ *     `chunk_size` are accepted and ignored (the reversed spectrum is the
+ *     conjugate of the forward one; the GPU schedules its own work).
+ *
+ *  2. Native entry points returning an int status (SEISMIC_OK == 0), taking
+ *     explicit sizes and strides, with channels, device-resident buffers and
+ *     caller-provided streams.  They have no counterpart in the reference's
+ *     ABI beyond the computation itself (correlation_c.cpp:58-137,251-293),
+ *     whose semantics they keep.
+ *
+ * Semantics shared by all entry points (reference: correlation_c.cpp):
+ *  - pairs (i, j >= i) of the upper triangle including the diagonal, packed
+ *    row-major at index i*N - i*(i-1)/2 + (j-i) (:269), 64-bit;
+ *  - lags d = 1-shift .. shift, series value at lag d = sum_k x_i[k] x_j[k-d]
+ *    (circular of size paddedSize), first strict maximum above 0 / minimum
+ *    below 0 in increasing d, else value 0 and lag 0 (:102-111);
+ *  - coefficient = peak / (paddedSize * |x_i| * |x_j|), norms in FP64
+ *    (:115,:127); with C > 1 channels, the mean over channels of the
+ *    per-channel normalised series;
+ *  - histograms count every pair before thresholding: last bin for
+ *    |coef| >= 1, else int(|coef| / float(1.0/n_classes_hist)) (:116-117,
+ *    :128-129), accumulated into the caller's arrays;
+ *  - threshold: coef > threshold (max) / coef < -threshold (min) are kept,
+ *    others become 0 with lag 0 (:119-136);
+ *  - a pair with a zero-norm event (all channels) reports 0 / 0 and is
+ *    counted in no histogram bin (the reference divides by zero there).
+ */
+#ifndef SEISMIC_GB300_H
+#define SEISMIC_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SEISMIC_OK 0
+#define SEISMIC_ERR_INVALID_ARGUMENT 1
+#define SEISMIC_ERR_UNSUPPORTED_SIZE 2
+#define SEISMIC_ERR_OUT_OF_MEMORY 3
+#define SEISMIC_ERR_CUDA 4
+#define SEISMIC_ERR_NO_DEVICE 5
+#define SEISMIC_ERR_WORKSPACE_TOO_SMALL 6
+
+/* ---- computation forms -------------------------------------------------- */
+#define SEISMIC_FORM_FP32 0 /* FP32 spectra, FP32 products, FP32 inverse FFT */
+
+/* ---- drop-in symbols (reference ABI) ----------------------------------- */
+
+/* Replaces correlationCPP, Correlation_in_OMP/correlation_c.cpp:210-213. */
+void correlationCPP(float *events, float *events_reversed, int n_events, int event_length, int shift,
+                    int paddedSize, int num_threads, int chunk_size, float threshold,
+                    int n_classes_hist, float *xcorr_vals_pos, int *xcorr_lags_pos,
+                    float *xcorr_vals_neg, int *xcorr_lags_neg, int *max_hist, int *min_hist);
+
+/* Replaces correlationCUDA, Correlation_in_CUDA/correlation_cuda.cu:530-533
+ * (OpenMP-path semantics: below-threshold outputs are written as 0). */
+void correlationCUDA(float *events, float *events_reversed, int n_events, int event_length, int shift,
+                     int paddedSize, int num_threads, float threshold, float *xcorr_vals_pos,
+                     int *xcorr_lags_pos, float *xcorr_vals_neg, int *xcorr_lags_neg);
+
+/* Replaces initialiseCUDA, Correlation_in_CUDA/correlation_cuda.cu:509-527:
+ * creates the context and loads the kernels so the first call is not
+ * charged for it. */
+void initialiseCUDA(void);
+
+/* ---- errors ------------------------------------------------------------ */
+
+/* Status of the calling thread's last call into this library. */
+int seismic_last_error(void);
+/* Human-readable message for the calling thread's last error ("" if none). */
+const char *seismic_last_error_message(void);
+const char *seismic_status_string(int status);
+
+/* ---- native entry points ------------------------------------------------ */
+
+/* Padded FFT size used when a native call passes padded_size = 0: the
+ * smallest power of two >= event_length + shift (exact linear correlation
+ * over the whole lag window).  Returns 0 if that exceeds the supported
+ * maximum (8192). */
+int seismic_resolve_padded_size(int event_length, int shift);
+
+/* Device workspace (bytes) seismic_xcorr_device needs for these sizes. */
+size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int padded_size, int form);
+
+/* All-pairs correlation of device-resident events.
+ *   d_events: element (e, c, s) at d_events[e*event_stride + c*channel_stride + s],
+ *             s < event_length (samples beyond are treated as zero);
+ *   outputs:  device arrays of n_events*(n_events+1)/2 entries (packed triangle);
+ *   d_max_hist/d_min_hist: device int[n_classes_hist], accumulated into, or
+ *             NULL with n_classes_hist == 0;
+ *   workspace: device buffer of seismic_xcorr_workspace_bytes() or NULL (the
+ *             library then uses its own cached allocation);
+ *   stream:   a cudaStream_t (NULL = legacy default stream).
+ * Asynchronous with respect to the host.  Returns a SEISMIC_* status. */
+int seismic_xcorr_device(const float *d_events, long long n_events, int n_channels, int event_length,
+                         long long event_stride, long long channel_stride, int padded_size, int shift,
+                         float threshold, int n_classes_hist, int form, float *d_vals_pos,
+                         int *d_lags_pos, float *d_vals_neg, int *d_lags_neg, int *d_max_hist,
+                         int *d_min_hist, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Same computation from host memory (pinned or pageable) into host memory,
+ * synchronous: copies events in, runs, copies the packed outputs back and
+ * adds the histograms into max_hist/min_hist (may be NULL if
+ * n_classes_hist == 0).  Host events use the strides of seismic_xcorr_device
+ * with event_stride == n_channels * channel_stride. */
+int seismic_xcorr_host(const float *events, long long n_events, int n_channels, int event_length,
+                       long long event_stride, long long channel_stride, int padded_size, int shift,
+                       float threshold, int n_classes_hist, int form, float *vals_pos, int *lags_pos,
+                       float *vals_neg, int *lags_neg, int *max_hist, int *min_hist);
+
+/* Kernel (a) alone: packed half spectra and FP64 norms of every (event,
+ * channel) row.  d_spectra: n_events*n_channels rows of padded_size/2
+ * float2 (slot 0 = (Re X[0], Re X[P/2]), slot k = X[k]); d_norms:
+ * n_events*n_channels doubles.  prescale != 0 scales each row by 1/norm
+ * (0 for a zero row), the form the multichannel mean uses. */
+int seismic_spectra_device(const float *d_events, long long n_events, int n_channels, int event_length,
+                           long long event_stride, long long channel_stride, int padded_size, int prescale,
+                           void *d_spectra, double *d_norms, void *stream);
+
+/* Kernel (b) alone: all pairs of the upper triangle from spectra made by
+ * seismic_spectra_device with the same padded_size (prescale must be set
+ * when n_channels > 1).  Outputs and histograms as seismic_xcorr_device. */
+int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long n_events, int n_channels,
+                         int padded_size, int prescaled, int shift, float threshold, int n_classes_hist,
+                         int form, float *d_vals_pos, int *d_lags_pos, float *d_vals_neg, int *d_lags_neg,
+                         int *d_max_hist, int *d_min_hist, void *stream);
+
+/* Number of kernels this library has launched in this process. */
+unsigned long long seismic_launch_count(void);
+
+/* Releases the library's cached device buffers on the current device. */
+int seismic_release_cached_memory(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEISMIC_GB300_H */

@@ -1,0 +1,430 @@
+// C ABI of libseismic_gb300.so: drop-in reference symbols and native entry
+// points (declared in include/seismic_gb300.h).
+//
+// Host-side flow of one correlation (replacing correlationCUDA,
+// Correlation_in_CUDA/correlation_cuda.cu:530-673, and correlationCPP,
+// Correlation_in_OMP/correlation_c.cpp:210-298):
+//   H2D of the L valid samples of every event row (one 2-D copy)
+//   kernel (a) spectra_kernel : packed half spectra + FP64 norms
+//   kernel (b) pair_kernel    : all pairs of the upper triangle
+//   D2H of the four packed outputs and the histograms.
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/seismic_gb300.h"
+#include "kernels.cuh"
+
+namespace seismic {
+
+// ------------------------------------------------------------------ errors
+static thread_local int tl_status = SEISMIC_OK;
+static thread_local char tl_message[512] = {0};
+
+static int set_status(int status, const char *fmt, ...) {
+  tl_status = status;
+  if (status == SEISMIC_OK) {
+    tl_message[0] = 0;
+    return status;
+  }
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(tl_message, sizeof(tl_message), fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+static int cuda_status(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return SEISMIC_OK;
+  if (e == cudaErrorMemoryAllocation)
+    return set_status(SEISMIC_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    return set_status(SEISMIC_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+  return set_status(SEISMIC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define SEISMIC_TRY(expr, what)                          \
+  do {                                                   \
+    cudaError_t e__ = (expr);                            \
+    if (e__ != cudaSuccess) return cuda_status(e__, what); \
+  } while (0)
+
+static std::atomic<unsigned long long> g_launches{0};
+
+// ----------------------------------------------------------- device state
+struct DeviceState {
+  bool ready = false;
+  int sm_count = 0;
+  const float2 *twiddles = nullptr;
+  cudaStream_t stream = nullptr;
+  // grow-only cached buffers used when the caller passes none
+  void *ws = nullptr;
+  size_t ws_bytes = 0;
+  void *io = nullptr;  // events + outputs + histograms for the host entry point
+  size_t io_bytes = 0;
+};
+
+static std::mutex g_mutex;
+static std::vector<DeviceState> g_devices;
+
+static int ensure_device(int *dev_out, DeviceState **st_out) {
+  int dev = 0;
+  SEISMIC_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if ((int)g_devices.size() <= dev) g_devices.resize(dev + 1);
+  DeviceState &st = g_devices[dev];
+  if (!st.ready) {
+    SEISMIC_TRY(cudaDeviceGetAttribute(&st.sm_count, cudaDevAttrMultiProcessorCount, dev),
+                "cudaDeviceGetAttribute");
+    SEISMIC_TRY(cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    SEISMIC_TRY(init_twiddles(st.stream), "twiddle init");
+    g_launches.fetch_add(1);
+    SEISMIC_TRY(cudaStreamSynchronize(st.stream), "twiddle init sync");
+    st.twiddles = twiddle_table();
+    if (!st.twiddles) return set_status(SEISMIC_ERR_CUDA, "twiddle table address");
+    st.ready = true;
+  }
+  *dev_out = dev;
+  *st_out = &st;
+  return SEISMIC_OK;
+}
+
+static int grow(void **ptr, size_t *have, size_t need, const char *what) {
+  if (*have >= need && *ptr) return SEISMIC_OK;
+  if (*ptr) {
+    cudaFree(*ptr);
+    *ptr = nullptr;
+    *have = 0;
+  }
+  SEISMIC_TRY(cudaMalloc(ptr, need), what);
+  *have = need;
+  return SEISMIC_OK;
+}
+
+static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+static size_t spectra_bytes(long long rows, int P) { return align256((size_t)rows * (size_t)(P / 2) * sizeof(float2)); }
+static size_t norms_bytes(long long rows) { return align256((size_t)rows * sizeof(double)); }
+
+static int validate(long long n_events, int n_channels, int event_length, int padded, int shift,
+                    int n_hist, int form) {
+  if (n_events < 1) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_events must be >= 1 (got %lld)", n_events);
+  if (n_channels < 1) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_channels must be >= 1");
+  if (event_length < 1) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "event_length must be >= 1");
+  if (!supported_padded_size(padded))
+    return set_status(SEISMIC_ERR_UNSUPPORTED_SIZE, "paddedSize %d unsupported (power of two in [64, 8192])", padded);
+  if (event_length > padded)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "event_length %d exceeds paddedSize %d", event_length, padded);
+  if (shift < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "shift must be >= 0");
+  if (n_hist < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_classes_hist must be >= 0");
+  if (form != SEISMIC_FORM_FP32) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "unknown form %d", form);
+  // lag indices must fit in int32 alongside the sentinel values
+  if (shift > (1 << 29)) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "shift too large");
+  return SEISMIC_OK;
+}
+
+static int run_spectra(const DeviceState &st, const float *d_events, long long n, int C, int L, long long ev_stride,
+                       long long ch_stride, int P, int prescale, float2 *spectra, double *norms,
+                       cudaStream_t stream) {
+  SpectraArgs sa;
+  sa.events = d_events;
+  sa.n_events = n;
+  sa.n_channels = C;
+  sa.length = L;
+  sa.ev_stride = ev_stride;
+  sa.ch_stride = ch_stride;
+  sa.prescale = prescale;
+  sa.spectra = spectra;
+  sa.norms = norms;
+  sa.twiddles = st.twiddles;
+  SEISMIC_TRY(launch_spectra(P, sa, stream), "spectra kernel launch");
+  g_launches.fetch_add(1);
+  return SEISMIC_OK;
+}
+
+static int run_pairs(const DeviceState &st, const float2 *spectra, const double *norms, long long n, int C, int P,
+                     int prescaled, int shift, float thr, int n_hist, float *vp, int *lp, float *vn, int *ln,
+                     int *hmax, int *hmin, cudaStream_t stream) {
+  PairArgs pa;
+  pa.spectra = spectra;
+  pa.norms = norms;
+  pa.n_events = n;
+  pa.n_channels = C;
+  pa.shift = shift;
+  pa.prescaled = prescaled;
+  pa.threshold = thr;
+  pa.n_hist = n_hist;
+  pa.delta_hist = n_hist > 0 ? (float)(1.0 / n_hist) : 0.f;
+  pa.vals_pos = vp;
+  pa.lags_pos = lp;
+  pa.vals_neg = vn;
+  pa.lags_neg = ln;
+  pa.max_hist = hmax;
+  pa.min_hist = hmin;
+  pa.tile = pair_tile_for(P);
+  pa.twiddles = st.twiddles;
+  pa.couple_begin = 0;
+  pa.couple_end = pair_couples_total(n, pa.tile);
+  static int ctas_cache[16] = {0};
+  const int lp2 = 31 - __builtin_clz((unsigned)P);
+  if (!ctas_cache[lp2]) ctas_cache[lp2] = pair_ctas_per_sm(P);
+  const int G = P / 32;
+  const int NG = (256 / G) > 0 ? (256 / G) : 1;
+  long long want = (pa.couple_end + NG - 1) / NG;
+  long long grid = (long long)st.sm_count * ctas_cache[lp2];
+  if (want < grid) grid = want;
+  if (grid < 1) grid = 1;
+  SEISMIC_TRY(launch_pairs(P, pa, (int)grid, stream), "pair kernel launch");
+  g_launches.fetch_add(1);
+  return SEISMIC_OK;
+}
+
+// Core: spectra + pairs on `stream`; buffers all on device.
+static int run_xcorr(const DeviceState &st, const float *d_events, long long n, int C, int L, long long ev_stride,
+                     long long ch_stride, int P, int shift, float thr, int n_hist, float *vp, int *lp, float *vn,
+                     int *ln, int *hmax, int *hmin, void *ws, cudaStream_t stream) {
+  const long long rows = n * C;
+  float2 *spectra = reinterpret_cast<float2 *>(ws);
+  double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(ws) + spectra_bytes(rows, P));
+  const int prescale = C > 1 ? 1 : 0;
+  int s = run_spectra(st, d_events, n, C, L, ev_stride, ch_stride, P, prescale, spectra, norms, stream);
+  if (s) return s;
+  return run_pairs(st, spectra, norms, n, C, P, prescale, shift, thr, n_hist, vp, lp, vn, ln, hmax, hmin, stream);
+}
+
+}  // namespace seismic
+
+using namespace seismic;
+
+extern "C" {
+
+int seismic_last_error(void) { return tl_status; }
+const char *seismic_last_error_message(void) { return tl_message; }
+
+const char *seismic_status_string(int status) {
+  switch (status) {
+    case SEISMIC_OK: return "ok";
+    case SEISMIC_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case SEISMIC_ERR_UNSUPPORTED_SIZE: return "unsupported size";
+    case SEISMIC_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case SEISMIC_ERR_CUDA: return "CUDA error";
+    case SEISMIC_ERR_NO_DEVICE: return "no CUDA device";
+    case SEISMIC_ERR_WORKSPACE_TOO_SMALL: return "workspace too small";
+    default: return "unknown status";
+  }
+}
+
+unsigned long long seismic_launch_count(void) { return g_launches.load(); }
+
+int seismic_resolve_padded_size(int event_length, int shift) {
+  if (event_length < 1 || shift < 0) return 0;
+  long long need = (long long)event_length + shift;
+  long long p = kMinP;
+  while (p < need) p <<= 1;
+  return p <= kMaxP ? (int)p : 0;
+}
+
+size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int padded_size, int form) {
+  (void)form;
+  if (n_events < 1 || n_channels < 1 || !supported_padded_size(padded_size)) return 0;
+  const long long rows = n_events * n_channels;
+  return spectra_bytes(rows, padded_size) + norms_bytes(rows);
+}
+
+int seismic_xcorr_device(const float *d_events, long long n_events, int n_channels, int event_length,
+                         long long event_stride, long long channel_stride, int padded_size, int shift,
+                         float threshold, int n_classes_hist, int form, float *d_vals_pos, int *d_lags_pos,
+                         float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist, void *workspace,
+                         size_t workspace_bytes, void *stream) {
+  set_status(SEISMIC_OK, "");
+  if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  int s = validate(n_events, n_channels, event_length, padded_size, shift, n_classes_hist, form);
+  if (s) return s;
+  if (!d_events || !d_vals_pos || !d_lags_pos || !d_vals_neg || !d_lags_neg)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");
+  if (n_classes_hist > 0 && (!d_max_hist || !d_min_hist))
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null histogram buffer");
+  int dev;
+  DeviceState *st;
+  if ((s = ensure_device(&dev, &st))) return s;
+  const size_t need = seismic_xcorr_workspace_bytes(n_events, n_channels, padded_size, form);
+  if (workspace) {
+    if (workspace_bytes < need)
+      return set_status(SEISMIC_ERR_WORKSPACE_TOO_SMALL, "workspace %zu < %zu bytes", workspace_bytes, need);
+  } else {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if ((s = grow(&st->ws, &st->ws_bytes, need, "workspace allocation"))) return s;
+    workspace = st->ws;
+  }
+  return run_xcorr(*st, d_events, n_events, n_channels, event_length, event_stride, channel_stride, padded_size,
+                   shift, threshold, n_classes_hist, d_vals_pos, d_lags_pos, d_vals_neg, d_lags_neg, d_max_hist,
+                   d_min_hist, workspace, (cudaStream_t)stream);
+}
+
+int seismic_spectra_device(const float *d_events, long long n_events, int n_channels, int event_length,
+                           long long event_stride, long long channel_stride, int padded_size, int prescale,
+                           void *d_spectra, double *d_norms, void *stream) {
+  set_status(SEISMIC_OK, "");
+  int s = validate(n_events, n_channels, event_length, padded_size, 0, 0, SEISMIC_FORM_FP32);
+  if (s) return s;
+  if (!d_events || !d_spectra || !d_norms) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");
+  int dev;
+  DeviceState *st;
+  if ((s = ensure_device(&dev, &st))) return s;
+  return run_spectra(*st, d_events, n_events, n_channels, event_length, event_stride, channel_stride, padded_size,
+                     prescale ? 1 : 0, reinterpret_cast<float2 *>(d_spectra), d_norms, (cudaStream_t)stream);
+}
+
+int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long n_events, int n_channels,
+                         int padded_size, int prescaled, int shift, float threshold, int n_classes_hist, int form,
+                         float *d_vals_pos, int *d_lags_pos, float *d_vals_neg, int *d_lags_neg, int *d_max_hist,
+                         int *d_min_hist, void *stream) {
+  set_status(SEISMIC_OK, "");
+  int s = validate(n_events, n_channels, 1, padded_size, shift, n_classes_hist, form);
+  if (s) return s;
+  if (!d_spectra || !d_norms || !d_vals_pos || !d_lags_pos || !d_vals_neg || !d_lags_neg)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");
+  if (n_classes_hist > 0 && (!d_max_hist || !d_min_hist))
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null histogram buffer");
+  if (n_channels > 1 && !prescaled)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "multichannel spectra must be prescaled");
+  int dev;
+  DeviceState *st;
+  if ((s = ensure_device(&dev, &st))) return s;
+  return run_pairs(*st, reinterpret_cast<const float2 *>(d_spectra), d_norms, n_events, n_channels, padded_size,
+                   prescaled ? 1 : 0, shift, threshold, n_classes_hist, d_vals_pos, d_lags_pos, d_vals_neg,
+                   d_lags_neg, d_max_hist, d_min_hist, (cudaStream_t)stream);
+}
+
+int seismic_xcorr_host(const float *events, long long n_events, int n_channels, int event_length,
+                       long long event_stride, long long channel_stride, int padded_size, int shift,
+                       float threshold, int n_classes_hist, int form, float *vals_pos, int *lags_pos,
+                       float *vals_neg, int *lags_neg, int *max_hist, int *min_hist) {
+  set_status(SEISMIC_OK, "");
+  if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  int s = validate(n_events, n_channels, event_length, padded_size, shift, n_classes_hist, form);
+  if (s) return s;
+  if (!events || !vals_pos || !lags_pos || !vals_neg || !lags_neg)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");
+  if (n_classes_hist > 0 && (!max_hist || !min_hist))
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null histogram buffer");
+  if (event_stride != (long long)n_channels * channel_stride || channel_stride < event_length)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT,
+                      "host events need event_stride == n_channels*channel_stride >= n_channels*event_length");
+  int dev;
+  DeviceState *st;
+  if ((s = ensure_device(&dev, &st))) return s;
+
+  const long long rows = n_events * n_channels;
+  const long long npairs = n_events * (n_events + 1) / 2;
+  const size_t ev_b = align256((size_t)rows * event_length * sizeof(float));
+  const size_t out_b = align256((size_t)npairs * 4);
+  const size_t hist_b = align256((size_t)2 * (n_classes_hist > 0 ? n_classes_hist : 1) * sizeof(int));
+  const size_t ws_b = seismic_xcorr_workspace_bytes(n_events, n_channels, padded_size, form);
+  const size_t total = ev_b + 4 * out_b + hist_b + ws_b;
+
+  std::lock_guard<std::mutex> lock(g_mutex);  // the cached io buffer is shared
+  if ((s = grow(&st->io, &st->io_bytes, total, "device buffers for the host call"))) return s;
+  char *base = reinterpret_cast<char *>(st->io);
+  float *d_ev = reinterpret_cast<float *>(base);
+  float *d_vp = reinterpret_cast<float *>(base + ev_b);
+  int *d_lp = reinterpret_cast<int *>(base + ev_b + out_b);
+  float *d_vn = reinterpret_cast<float *>(base + ev_b + 2 * out_b);
+  int *d_ln = reinterpret_cast<int *>(base + ev_b + 3 * out_b);
+  int *d_hist = reinterpret_cast<int *>(base + ev_b + 4 * out_b);
+  void *d_ws = base + ev_b + 4 * out_b + hist_b;
+  cudaStream_t stream = st->stream;
+
+  SEISMIC_TRY(cudaMemcpy2DAsync(d_ev, (size_t)event_length * sizeof(float), events,
+                                (size_t)channel_stride * sizeof(float), (size_t)event_length * sizeof(float),
+                                (size_t)rows, cudaMemcpyHostToDevice, stream),
+              "events H2D");
+  if (n_classes_hist > 0)
+    SEISMIC_TRY(cudaMemsetAsync(d_hist, 0, 2 * (size_t)n_classes_hist * sizeof(int), stream), "hist clear");
+  s = run_xcorr(*st, d_ev, n_events, n_channels, event_length, (long long)n_channels * event_length, event_length,
+                padded_size, shift, threshold, n_classes_hist, d_vp, d_lp, d_vn, d_ln, d_hist,
+                d_hist + (n_classes_hist > 0 ? n_classes_hist : 0), d_ws, stream);
+  if (s) return s;
+  const size_t ob = (size_t)npairs * 4;
+  SEISMIC_TRY(cudaMemcpyAsync(vals_pos, d_vp, ob, cudaMemcpyDeviceToHost, stream), "vals_pos D2H");
+  SEISMIC_TRY(cudaMemcpyAsync(lags_pos, d_lp, ob, cudaMemcpyDeviceToHost, stream), "lags_pos D2H");
+  SEISMIC_TRY(cudaMemcpyAsync(vals_neg, d_vn, ob, cudaMemcpyDeviceToHost, stream), "vals_neg D2H");
+  SEISMIC_TRY(cudaMemcpyAsync(lags_neg, d_ln, ob, cudaMemcpyDeviceToHost, stream), "lags_neg D2H");
+  std::vector<int> h(n_classes_hist > 0 ? 2 * (size_t)n_classes_hist : 0);
+  if (n_classes_hist > 0)
+    SEISMIC_TRY(cudaMemcpyAsync(h.data(), d_hist, h.size() * sizeof(int), cudaMemcpyDeviceToHost, stream),
+                "hist D2H");
+  SEISMIC_TRY(cudaStreamSynchronize(stream), "host call sync");
+  for (int k = 0; k < n_classes_hist; ++k) {
+    max_hist[k] += h[k];
+    min_hist[k] += h[n_classes_hist + k];
+  }
+  return SEISMIC_OK;
+}
+
+int seismic_release_cached_memory(void) {
+  set_status(SEISMIC_OK, "");
+  int dev = 0;
+  SEISMIC_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if ((int)g_devices.size() > dev) {
+    DeviceState &st = g_devices[dev];
+    if (st.ws) cudaFree(st.ws);
+    if (st.io) cudaFree(st.io);
+    st.ws = st.io = nullptr;
+    st.ws_bytes = st.io_bytes = 0;
+  }
+  return SEISMIC_OK;
+}
+
+// ----------------------------------------------------- reference symbols
+static void report_legacy(const char *fn, int status) {
+  if (status != SEISMIC_OK) fprintf(stderr, "seismic_gb300 %s: %s\n", fn, tl_message);
+}
+
+void correlationCPP(float *events, float *events_reversed, int n_events, int event_length, int shift,
+                    int paddedSize, int num_threads, int chunk_size, float threshold, int n_classes_hist,
+                    float *xcorr_vals_pos, int *xcorr_lags_pos, float *xcorr_vals_neg, int *xcorr_lags_neg,
+                    int *max_hist, int *min_hist) {
+  (void)events_reversed;
+  (void)num_threads;
+  (void)chunk_size;
+  if (n_classes_hist < 1) {
+    set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_classes_hist must be >= 1");
+    report_legacy("correlationCPP", tl_status);
+    return;
+  }
+  const int s = seismic_xcorr_host(events, n_events, 1, event_length, paddedSize, paddedSize, paddedSize, shift,
+                                   threshold, n_classes_hist, SEISMIC_FORM_FP32, xcorr_vals_pos, xcorr_lags_pos,
+                                   xcorr_vals_neg, xcorr_lags_neg, max_hist, min_hist);
+  report_legacy("correlationCPP", s);
+}
+
+void correlationCUDA(float *events, float *events_reversed, int n_events, int event_length, int shift,
+                     int paddedSize, int num_threads, float threshold, float *xcorr_vals_pos, int *xcorr_lags_pos,
+                     float *xcorr_vals_neg, int *xcorr_lags_neg) {
+  (void)events_reversed;
+  (void)num_threads;
+  const int s = seismic_xcorr_host(events, n_events, 1, event_length, paddedSize, paddedSize, paddedSize, shift,
+                                   threshold, 0, SEISMIC_FORM_FP32, xcorr_vals_pos, xcorr_lags_pos, xcorr_vals_neg,
+                                   xcorr_lags_neg, nullptr, nullptr);
+  report_legacy("correlationCUDA", s);
+}
+
+void initialiseCUDA(void) {
+  set_status(SEISMIC_OK, "");
+  int dev;
+  DeviceState *st;
+  const int s = ensure_device(&dev, &st);
+  if (s == SEISMIC_OK) {
+    for (int P = kMinP; P <= kMaxP; P <<= 1) pair_ctas_per_sm(P);  // loads the kernels
+  }
+  report_legacy("initialiseCUDA", s);
+}
+
+}  // extern "C"

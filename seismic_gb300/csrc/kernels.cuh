@@ -1,0 +1,69 @@
+// Kernel declarations and launch helpers shared by the C-ABI layer.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace seismic {
+
+constexpr int kMaxP = 8192;  // largest supported padded FFT size
+constexpr int kMinP = 64;    // smallest
+
+// Layout of the packed half spectrum of one (event, channel) row:
+//   slot 0      = (Re X[0], Re X[P/2])   (both bins are real for real input)
+//   slot k>0    = X[k],  k = 1 .. P/2-1
+// Rows are [event][channel], each P/2 float2 = 4P bytes (16-byte aligned).
+
+struct SpectraArgs {
+  const float *events;     // time series, element (e, c, s) at events[e*ev_stride + c*ch_stride + s]
+  long long n_events;
+  int n_channels;
+  int length;              // L samples used (zero beyond)
+  long long ev_stride;     // elements
+  long long ch_stride;     // elements
+  int prescale;            // 1: spectra scaled by 1/norm (0 if norm == 0); 0: unscaled
+  float2 *spectra;         // out [n_events*n_channels][P/2]
+  double *norms;           // out [n_events*n_channels], FP64 L2 norms
+  const float2 *twiddles;  // twiddle_table()
+};
+
+struct PairArgs {
+  const float2 *spectra;   // [n_events*n_channels][P/2]
+  const double *norms;     // [n_events*n_channels]
+  long long n_events;
+  int n_channels;
+  int shift;               // lags d = 1-shift .. shift
+  int prescaled;           // spectra were scaled by 1/norm (multichannel mean)
+  float threshold;
+  int n_hist;              // 0 disables histograms
+  float delta_hist;        // float(1.0 / n_hist)
+  float *vals_pos;
+  int *lags_pos;
+  float *vals_neg;
+  int *lags_neg;
+  int *max_hist;           // device, accumulated into
+  int *min_hist;
+  // work range in couples (pairs of pairs), for chunked or sharded launches
+  long long couple_begin;
+  long long couple_end;
+  int tile;                // events per tile side
+  const float2 *twiddles;  // twiddle_table()
+};
+
+// Number of two-pair work items ("couples") covering the upper triangle of
+// n_events with square tiles of `tile` events.
+long long pair_couples_total(long long n_events, int tile);
+int pair_tile_for(int P);
+
+cudaError_t launch_spectra(int P, const SpectraArgs &a, cudaStream_t s);
+cudaError_t launch_pairs(int P, const PairArgs &a, int grid_ctas, cudaStream_t s);
+int pair_ctas_per_sm(int P);
+cudaError_t init_twiddles(cudaStream_t s);
+// Device address of the twiddle table exp(+2 pi i k / kMaxP) of the current
+// device (valid after init_twiddles on that device).
+const float2 *twiddle_table();
+
+bool supported_padded_size(int P);
+
+}  // namespace seismic

@@ -1,0 +1,391 @@
+// Kernels (b) + (c): fused pair-tile correlation with an upper-triangle tile
+// scheduler.
+//
+// Replaces, per pair (i, j >= i) of the packed upper triangle:
+//   ElementWiseMultiplication  Correlation_in_OMP/correlation_c.cpp:188-193
+//   inverseFFT (c2r + window scan + normalise + histogram + threshold)
+//                              Correlation_in_OMP/correlation_c.cpp:58-137
+//   the dynamic row loop       Correlation_in_OMP/correlation_c.cpp:251-293
+// and the GPU chunk loop EWM_Linear -> cuFFT C2R -> FE_Linear of
+// Correlation_in_CUDA/correlation_cuda.cu:409-505, without any lag series
+// or product spectrum ever written to global memory.
+//
+// Work decomposition.  Events are cut into square tiles of `tile` events;
+// tiles (bi, bj >= bi) are enumerated row-major over the upper triangle
+// (decode_tile).  A tile holds tile*tile/2 "couples": two pairs (i, j) and
+// (i, j+1) that share event i.  One couple is one size-P complex inverse FFT:
+//   Z = Y1 + i Y2,  Y1 = sum_c X_ic conj X_jc,  Y2 = sum_c X_ic conj X_(j+1)c,
+// and, because both lag series are real, Re z and Im z are the two series.
+// Couples are dealt to groups of G = P/32 threads round-robin; the groups of
+// one CTA take neighbouring couples of the same tile, so the tile's spectra
+// are re-read from L1.
+//
+// Lag semantics.  z[m] is the circular correlation sum_k x_i[k] x_j[k-d] at
+// d = m (mod P).  The reference scans corr_t[L + t], t = -shift .. shift-1,
+// reporting lag t+1 (correlation_c.cpp:102-111); corr_t[L+t] equals the
+// circular correlation at d = t+1, so lag d is read at m = d mod P, and the
+// first-occurrence rule becomes "largest value, ties to the smallest d".
+#include <climits>
+
+#include "fft_core.cuh"
+#include "kernels.cuh"
+
+namespace seismic {
+
+constexpr int kSmemHistMax = 4096;
+
+__host__ __device__ __forceinline__ long long tri_start(long long b, long long nb) {
+  return b * nb - b * (b - 1) / 2;
+}
+
+// Row-major decode of tile index x over the upper triangle of nb x nb tiles.
+__device__ __forceinline__ void decode_tile(long long x, long long nb, long long &bi, long long &bj) {
+  const double twonb1 = 2.0 * (double)nb + 1.0;
+  long long b = (long long)((twonb1 - sqrt(twonb1 * twonb1 - 8.0 * (double)x)) * 0.5);
+  if (b < 0) b = 0;
+  if (b > nb - 1) b = nb - 1;
+  while (b + 1 < nb && tri_start(b + 1, nb) <= x) ++b;
+  while (b > 0 && tri_start(b, nb) > x) --b;
+  bi = b;
+  bj = b + (x - tri_start(b, nb));
+}
+
+long long pair_couples_total(long long n_events, int tile) {
+  const long long nb = (n_events + tile - 1) / tile;
+  return nb * (nb + 1) / 2 * ((long long)tile * tile / 2);
+}
+
+int pair_tile_for(int P) { return P <= 2048 ? 8 : (P == 4096 ? 4 : 2); }
+
+// Accumulate sum_c X_i conj X_j over channels: y += a * conj(b)
+__device__ __forceinline__ void cmac_conj(float2 &y, float2 a, float2 b) {
+  y.x = fmaf(a.x, b.x, fmaf(a.y, b.y, y.x));
+  y.y = fmaf(a.y, b.x, fmaf(-a.x, b.y, y.y));
+}
+
+struct Best {
+  float v;  // value (>= 0 for max, <= 0 for min)
+  int d;    // lag, INT_MIN while v == 0
+};
+
+__device__ __forceinline__ void upd_max(Best &b, float v, int d) {
+  if (v > b.v || (v == b.v && d < b.d)) { b.v = v; b.d = d; }
+}
+__device__ __forceinline__ void upd_min(Best &b, float v, int d) {
+  if (v < b.v || (v == b.v && d < b.d)) { b.v = v; b.d = d; }
+}
+
+__device__ __forceinline__ int hist_bin(float v, float delta, int n_hist) {
+  if (v >= 1.0f) return n_hist - 1;
+  int b = (int)(v / delta);
+  return b > n_hist - 1 ? n_hist - 1 : (b < 0 ? 0 : b);
+}
+
+template <int P>
+__global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  constexpr int S = P / 16;
+  constexpr int H = P / 2;
+  constexpr int NW = (G + 31) / 32;
+  using PL = FftPlan<P>;
+  constexpr int RL = PL::R4 ? PL::R4 : (PL::R3 ? PL::R3 : PL::R2);
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *bufs = reinterpret_cast<float2 *>(smem_raw);
+  unsigned *reds = reinterpret_cast<unsigned *>(bufs + NG * padded_len<P>());
+  int *hist = reinterpret_cast<int *>(reds + NG * NW * 8);
+
+  const int g = threadIdx.x / G;
+  const int t = threadIdx.x % G;
+  float2 *buf = bufs + g * padded_len<P>();
+  unsigned *red = reds + g * NW * 8;
+
+  const bool smem_hist = a.n_hist > 0 && a.n_hist <= kSmemHistMax;
+  if (smem_hist) {
+    for (int h = threadIdx.x; h < 2 * a.n_hist; h += blockDim.x) hist[h] = 0;
+  }
+  __syncthreads();
+
+  const long long N = a.n_events;
+  const int C = a.n_channels;
+  const long long T = a.tile;
+  const long long nb = (N + T - 1) / T;
+  const long long cpt = T * T / 2;
+  const long long stride = (long long)gridDim.x * NG;
+  const int d0 = 1 - a.shift;
+  const unsigned gmask = group_lane_mask<G>();
+
+  const int ca = (t == 0) ? 0 : t;
+  const int cb = (t == 0) ? S / 2 : S - t;
+
+  for (long long w = a.couple_begin + (long long)blockIdx.x * NG + g; w < a.couple_end; w += stride) {
+    const long long tile = w / cpt;
+    const long long lc = w - tile * cpt;
+    long long bi, bj;
+    decode_tile(tile, nb, bi, bj);
+    const long long ii = (2 * lc) / T, jj = (2 * lc) % T;
+    const long long i = bi * T + ii;
+    const long long j1 = bj * T + jj, j2 = j1 + 1;
+    const bool v1 = i < N && j1 < N && j1 >= i;
+    const bool v2 = i < N && j2 < N && j2 >= i;
+    if (!v1 && !v2) continue;  // uniform over the group
+    const long long ja = v1 ? j1 : j2;
+    const long long jb = j2 < N ? j2 : ja;
+    const bool out_b = v1 && v2;
+
+    // ---- conj products, accumulated over channels, for this thread's 16 bins
+    float2 ya1[8], ya2[8], yb1[8], yb2[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      ya1[r] = ya2[r] = yb1[r] = yb2[r] = make_float2(0.f, 0.f);
+    }
+    float dc1 = 0.f, dc2 = 0.f, nq1 = 0.f, nq2 = 0.f;
+    for (int c = 0; c < C; ++c) {
+      const float2 *Xi = a.spectra + (i * C + c) * (long long)H;
+      const float2 *X1 = a.spectra + (ja * C + c) * (long long)H;
+      const float2 *X2 = a.spectra + (jb * C + c) * (long long)H;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int ka = ca + r * S, kb = cb + r * S;
+        const float2 xa = __ldg(Xi + ka), pa = __ldg(X1 + ka), qa = __ldg(X2 + ka);
+        const float2 xb = __ldg(Xi + kb), pb = __ldg(X1 + kb), qb = __ldg(X2 + kb);
+        cmac_conj(ya1[r], xa, pa);
+        cmac_conj(ya2[r], xa, qa);
+        cmac_conj(yb1[r], xb, pb);
+        cmac_conj(yb2[r], xb, qb);
+        if (r == 0) {
+          dc1 = fmaf(xa.x, pa.x, dc1);
+          nq1 = fmaf(xa.y, pa.y, nq1);
+          dc2 = fmaf(xa.x, qa.x, dc2);
+          nq2 = fmaf(xa.y, qa.y, nq2);
+        }
+      }
+    }
+
+    // ---- assemble Z = Y1 + i Y2 over the full Hermitian range for columns a, b
+    float2 v[32];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const float2 A1 = ya1[r], A2 = ya2[r], B1 = yb1[r], B2 = yb2[r];
+      // Y1 + i Y2  and  conj(Y1) + i conj(Y2)
+      const float2 za = make_float2(A1.x - A2.y, A1.y + A2.x);
+      const float2 zac = make_float2(A1.x + A2.y, A2.x - A1.y);
+      const float2 zb = make_float2(B1.x - B2.y, B1.y + B2.x);
+      const float2 zbc = make_float2(B1.x + B2.y, B2.x - B1.y);
+      v[16 + r] = zb;
+      if (t != 0) {
+        v[r] = za;
+        v[16 + 15 - r] = zac;
+        v[15 - r] = zbc;
+      } else {
+        v[16 + 15 - r] = zbc;
+        if (r == 0) {
+          v[0] = make_float2(dc1, dc2);
+          v[8] = make_float2(nq1, nq2);
+        } else {
+          v[r] = za;
+          v[16 - r] = zac;
+        }
+      }
+    }
+
+    // ---- pass 1 (radix 16, no twiddles) on both columns, then Stockham passes
+    dft<16, 1>(&v[0]);
+    dft<16, 1>(&v[16]);
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      buf[pad16(ca * 16 + r)] = v[r];
+      buf[pad16(cb * 16 + r)] = v[16 + r];
+    }
+    group_sync<G>(g);
+    pass_read<P, PL::R2>(buf, v, t);
+    group_sync<G>(g);
+    pass_compute<P, PL::R2, 16, 1>(v, t, a.twiddles);
+    if constexpr (PL::R3 != 0) {
+      pass_write<P, PL::R2, 16>(buf, v, t);
+      group_sync<G>(g);
+      pass_read<P, PL::R3>(buf, v, t);
+      group_sync<G>(g);
+      pass_compute<P, PL::R3, 16 * PL::R2, 1>(v, t, a.twiddles);
+      if constexpr (PL::R4 != 0) {
+        pass_write<P, PL::R3, 16 * PL::R2>(buf, v, t);
+        group_sync<G>(g);
+        pass_read<P, PL::R4>(buf, v, t);
+        group_sync<G>(g);
+        pass_compute<P, PL::R4, 16 * PL::R2 * PL::R3, 1>(v, t, a.twiddles);
+      }
+    }
+
+    // ---- window scan straight from the last pass's registers
+    Best pa{0.f, INT_MIN}, na{0.f, INT_MIN}, pb{0.f, INT_MIN}, nb2{0.f, INT_MIN};
+#pragma unroll
+    for (int q = 0; q < 32 / RL; ++q) {
+#pragma unroll
+      for (int r = 0; r < RL; ++r) {
+        const int m = last_pass_index<P, RL>(t, q, r);
+        const int d = d0 + ((m - d0) & (P - 1));
+        if (d <= a.shift) {
+          const float2 z = v[q * RL + r];
+          upd_max(pa, z.x, d);
+          upd_min(na, z.x, d);
+          upd_max(pb, z.y, d);
+          upd_min(nb2, z.y, d);
+        }
+      }
+    }
+
+    // ---- group argmax / argmin: value by redux.max on the float bits
+    //      (all candidates are >= 0), then the smallest lag among the winners
+    unsigned key[4] = {__float_as_uint(pa.v), __float_as_uint(fabsf(na.v)), __float_as_uint(pb.v),
+                       __float_as_uint(fabsf(nb2.v))};
+    int lag[4] = {pa.d, na.d, pb.d, nb2.d};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const unsigned kmax = __reduce_max_sync(gmask, key[k]);
+      lag[k] = __reduce_min_sync(gmask, key[k] == kmax ? lag[k] : INT_MAX);
+      key[k] = kmax;
+    }
+    if constexpr (NW > 1) {
+      if ((t & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          red[(t >> 5) * 8 + k] = key[k];
+          red[(t >> 5) * 8 + 4 + k] = (unsigned)lag[k];
+        }
+      }
+      group_sync<G>(g);
+      if (t == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          for (int wv = 1; wv < NW; ++wv) {
+            const unsigned kk = red[wv * 8 + k];
+            const int ll = (int)red[wv * 8 + 4 + k];
+            if (kk > key[k] || (kk == key[k] && ll < lag[k])) { key[k] = kk; lag[k] = ll; }
+          }
+        }
+      }
+      group_sync<G>(g);
+    }
+
+    // ---- epilogue: normalise (FP64), histogram, threshold, packed write
+    if (t == 0) {
+#pragma unroll
+      for (int p = 0; p < 2; ++p) {
+        if (p == 1 && !out_b) break;
+        const long long j = p == 0 ? ja : jb;
+        const unsigned kp = key[2 * p], kn = key[2 * p + 1];
+        double denom;
+        bool live = false;
+        if (a.prescaled) {
+          for (int c = 0; c < C; ++c) live |= (a.norms[i * C + c] > 0.0) && (a.norms[j * C + c] > 0.0);
+          denom = (double)P * (double)C;
+        } else {
+          const double ni = a.norms[i * C], nj = a.norms[j * C];
+          live = ni > 0.0 && nj > 0.0;
+          denom = (double)P * ni * nj;
+        }
+        float vp = 0.f, vn = 0.f;
+        int lp = 0, ln = 0;
+        if (live) {
+          vp = (float)((double)__uint_as_float(kp) / denom);
+          vn = -(float)((double)__uint_as_float(kn) / denom);
+          lp = kp ? lag[2 * p] : 0;
+          ln = kn ? lag[2 * p + 1] : 0;
+          if (a.n_hist > 0) {
+            const int hp = hist_bin(vp, a.delta_hist, a.n_hist);
+            const int hn = hist_bin(-vn, a.delta_hist, a.n_hist);
+            if (smem_hist) {
+              atomicAdd(&hist[hp], 1);
+              atomicAdd(&hist[a.n_hist + hn], 1);
+            } else {
+              atomicAdd(&a.max_hist[hp], 1);
+              atomicAdd(&a.min_hist[hn], 1);
+            }
+          }
+          if (!(vp > a.threshold)) { vp = 0.f; lp = 0; }
+          if (!(vn < -a.threshold)) { vn = 0.f; ln = 0; }
+        }
+        const long long idx = i * N - i * (i - 1) / 2 + (j - i);
+        a.vals_pos[idx] = vp;
+        a.lags_pos[idx] = lp;
+        a.vals_neg[idx] = vn;
+        a.lags_neg[idx] = ln;
+      }
+    }
+  }
+
+  if (smem_hist) {
+    __syncthreads();
+    for (int h = threadIdx.x; h < a.n_hist; h += blockDim.x) {
+      if (hist[h]) atomicAdd(&a.max_hist[h], hist[h]);
+      if (hist[a.n_hist + h]) atomicAdd(&a.min_hist[h], hist[a.n_hist + h]);
+    }
+  }
+}
+
+template <int P> static size_t pair_smem_bytes(int n_hist) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  constexpr int NW = (G + 31) / 32;
+  size_t s = (size_t)NG * padded_len<P>() * sizeof(float2) + (size_t)NG * NW * 8 * sizeof(unsigned);
+  if (n_hist > 0 && n_hist <= kSmemHistMax) s += (size_t)2 * n_hist * sizeof(int);
+  return s;
+}
+
+template <int P> static cudaError_t launch_pairs_t(const PairArgs &a, int grid, cudaStream_t s) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  const size_t smem = pair_smem_bytes<P>(a.n_hist);
+  static int configured_bytes = 0;
+  if ((int)smem > configured_bytes) {
+    const int want = (int)pair_smem_bytes<P>(kSmemHistMax);
+    cudaError_t e = cudaFuncSetAttribute(pair_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+    if (e != cudaSuccess) return e;
+    configured_bytes = want;
+  }
+  if (a.couple_end <= a.couple_begin) return cudaSuccess;
+  pair_kernel<P><<<grid, NG * G, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <int P> static int ctas_per_sm_t() {
+  int n = 0;
+  const size_t smem = pair_smem_bytes<P>(64);
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  cudaFuncSetAttribute(pair_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)pair_smem_bytes<P>(kSmemHistMax));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_kernel<P>, NG * G, smem) != cudaSuccess) n = 1;
+  return n > 0 ? n : 1;
+}
+
+int pair_ctas_per_sm(int P) {
+  switch (P) {
+    case 64: return ctas_per_sm_t<64>();
+    case 128: return ctas_per_sm_t<128>();
+    case 256: return ctas_per_sm_t<256>();
+    case 512: return ctas_per_sm_t<512>();
+    case 1024: return ctas_per_sm_t<1024>();
+    case 2048: return ctas_per_sm_t<2048>();
+    case 4096: return ctas_per_sm_t<4096>();
+    case 8192: return ctas_per_sm_t<8192>();
+    default: return 1;
+  }
+}
+
+cudaError_t launch_pairs(int P, const PairArgs &a, int grid, cudaStream_t s) {
+  switch (P) {
+    case 64: return launch_pairs_t<64>(a, grid, s);
+    case 128: return launch_pairs_t<128>(a, grid, s);
+    case 256: return launch_pairs_t<256>(a, grid, s);
+    case 512: return launch_pairs_t<512>(a, grid, s);
+    case 1024: return launch_pairs_t<1024>(a, grid, s);
+    case 2048: return launch_pairs_t<2048>(a, grid, s);
+    case 4096: return launch_pairs_t<4096>(a, grid, s);
+    case 8192: return launch_pairs_t<8192>(a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace seismic

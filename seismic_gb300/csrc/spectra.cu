@@ -1,0 +1,201 @@
+// Kernel (a): forward real FFT of every (event, channel) row plus its FP64
+// energy norm, run once per row.
+//
+// Replaces the reference's ComputeNorms (Correlation_in_OMP/correlation_c.cpp:195-204,
+// float accumulation) and its two r2c FFT sets of the events and of the
+// time-reversed events (ComputeFFT, correlation_c.cpp:32-49; cuFFT R2C x2 in
+// Correlation_in_CUDA/correlation_cuda.cu:619-636).  Only the forward spectra
+// are built: the reversed-event spectrum is conj(X) times a linear phase, and
+// the pair kernel uses conj(X_j) directly.
+//
+// One group of G = P/32 threads transforms two rows at once as the real and
+// imaginary parts of one complex size-P FFT:
+//   z = a + i b,  Z = FFT(z),  A[k] = (Z[k] + conj Z[P-k]) / 2,
+//   B[k] = (Z[k] - conj Z[P-k]) / (2i).
+#include "fft_core.cuh"
+#include "kernels.cuh"
+
+namespace seismic {
+
+// exp(+2 pi i k / kMaxP); read by every kernel through a pointer argument.
+__device__ float2 g_twiddle[kMaxP];
+
+__global__ void twiddle_init_kernel() {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < kMaxP) {
+    double s, c;
+    sincospi(2.0 * (double)k / (double)kMaxP, &s, &c);
+    g_twiddle[k] = make_float2((float)c, (float)s);
+  }
+}
+
+cudaError_t init_twiddles(cudaStream_t s) {
+  twiddle_init_kernel<<<kMaxP / 256, 256, 0, s>>>();
+  return cudaGetLastError();
+}
+
+const float2 *twiddle_table() {
+  void *p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_twiddle) != cudaSuccess) return nullptr;
+  return reinterpret_cast<const float2 *>(p);
+}
+
+template <int G> __device__ __forceinline__ double group_sum_double(double v, double *red, int g, int t) {
+#pragma unroll
+  for (int o = (G < 32 ? G : 32) / 2; o > 0; o >>= 1) v += __shfl_xor_sync(group_lane_mask<G>(), v, o);
+  if constexpr (G > 32) {
+    if ((t & 31) == 0) red[t >> 5] = v;
+    group_sync<G>(g);
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < G / 32; ++w) s += red[w];
+    group_sync<G>(g);
+    return s;
+  } else {
+    return v;
+  }
+}
+
+template <int P>
+__global__ void __launch_bounds__(256) spectra_kernel(SpectraArgs a) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  constexpr int S = P / 16;
+  constexpr int H = P / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *bufs = reinterpret_cast<float2 *>(smem_raw);
+  double *reds = reinterpret_cast<double *>(bufs + NG * padded_len<P>());
+
+  const int g = threadIdx.x / G;
+  const int t = threadIdx.x % G;
+  float2 *buf = bufs + g * padded_len<P>();
+  double *red = reds + g * 2 * ((G + 31) / 32);
+
+  const long long rows = a.n_events * (long long)a.n_channels;
+  const long long row_a = 2 * ((long long)blockIdx.x * NG + g);
+  if (row_a >= rows) return;  // whole group leaves together
+  const long long row_b = row_a + 1;
+  const bool has_b = row_b < rows;
+
+  const float *src_a = a.events + (row_a / a.n_channels) * a.ev_stride + (row_a % a.n_channels) * a.ch_stride;
+  const float *src_b = has_b ? a.events + (row_b / a.n_channels) * a.ev_stride + (row_b % a.n_channels) * a.ch_stride
+                             : src_a;
+
+  // ---- pass 1: columns c0 = t and c1 = t + S/2, samples c + r*S
+  float2 v[32];
+  double ea = 0.0, eb = 0.0;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    const int c = t + half * (S / 2);
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int s = c + r * S;
+      float xa = 0.f, xb = 0.f;
+      if (s < a.length) {
+        xa = __ldg(src_a + s);
+        xb = has_b ? __ldg(src_b + s) : 0.f;
+      }
+      ea += (double)xa * (double)xa;
+      eb += (double)xb * (double)xb;
+      v[half * 16 + r] = make_float2(xa, xb);
+    }
+  }
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    dft<16, -1>(&v[half * 16]);
+    const int c = t + half * (S / 2);
+#pragma unroll
+    for (int r = 0; r < 16; ++r) buf[pad16(c * 16 + r)] = v[half * 16 + r];
+  }
+  ea = group_sum_double<G>(ea, red, g, t);
+  eb = group_sum_double<G>(eb, red, g, t);
+  group_sync<G>(g);
+
+  using PL = FftPlan<P>;
+  pass_read<P, PL::R2>(buf, v, t);
+  group_sync<G>(g);
+  pass_compute<P, PL::R2, 16, -1>(v, t, a.twiddles);
+  pass_write<P, PL::R2, 16>(buf, v, t);
+  group_sync<G>(g);
+  if constexpr (PL::R3 != 0) {
+    pass_read<P, PL::R3>(buf, v, t);
+    group_sync<G>(g);
+    pass_compute<P, PL::R3, 16 * PL::R2, -1>(v, t, a.twiddles);
+    pass_write<P, PL::R3, 16 * PL::R2>(buf, v, t);
+    group_sync<G>(g);
+  }
+  if constexpr (PL::R4 != 0) {
+    pass_read<P, PL::R4>(buf, v, t);
+    group_sync<G>(g);
+    pass_compute<P, PL::R4, 16 * PL::R2 * PL::R3, -1>(v, t, a.twiddles);
+    pass_write<P, PL::R4, 16 * PL::R2 * PL::R3>(buf, v, t);
+    group_sync<G>(g);
+  }
+
+  // ---- split the two rows, scale, write packed half spectra
+  const double na = sqrt(ea), nb = sqrt(eb);
+  float sa = 1.f, sb = 1.f;
+  if (a.prescale) {
+    sa = na > 0.0 ? (float)(1.0 / na) : 0.f;
+    sb = nb > 0.0 ? (float)(1.0 / nb) : 0.f;
+  }
+  float2 *dst_a = a.spectra + row_a * (long long)H;
+  float2 *dst_b = a.spectra + row_b * (long long)H;
+#pragma unroll 4
+  for (int k = t; k < H; k += G) {
+    const float2 zk = buf[pad16(k)];
+    if (k == 0) {
+      const float2 zh = buf[pad16(H)];
+      dst_a[0] = make_float2(zk.x * sa, zh.x * sa);
+      if (has_b) dst_b[0] = make_float2(zk.y * sb, zh.y * sb);
+    } else {
+      const float2 zm = buf[pad16(P - k)];
+      // A = (Z[k] + conj Z[P-k]) / 2 ; B = (Z[k] - conj Z[P-k]) / (2i)
+      const float2 A = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+      const float2 B = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+      dst_a[k] = make_float2(A.x * sa, A.y * sa);
+      if (has_b) dst_b[k] = make_float2(B.x * sb, B.y * sb);
+    }
+  }
+  if (t == 0) {
+    a.norms[row_a] = na;
+    if (has_b) a.norms[row_b] = nb;
+  }
+}
+
+template <int P> static cudaError_t launch_spectra_t(const SpectraArgs &a, cudaStream_t s) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  const long long rows = a.n_events * (long long)a.n_channels;
+  const long long groups = (rows + 1) / 2;
+  const long long ctas = (groups + NG - 1) / NG;
+  if (ctas <= 0) return cudaSuccess;
+  if (ctas > 0x7fffffffLL) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)NG * padded_len<P>() * sizeof(float2) + (size_t)NG * 2 * ((G + 31) / 32) * sizeof(double);
+  static bool configured = false;  // benign race: idempotent attribute set
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(spectra_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  spectra_kernel<P><<<(unsigned)ctas, NG * G, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spectra(int P, const SpectraArgs &a, cudaStream_t s) {
+  switch (P) {
+    case 64: return launch_spectra_t<64>(a, s);
+    case 128: return launch_spectra_t<128>(a, s);
+    case 256: return launch_spectra_t<256>(a, s);
+    case 512: return launch_spectra_t<512>(a, s);
+    case 1024: return launch_spectra_t<1024>(a, s);
+    case 2048: return launch_spectra_t<2048>(a, s);
+    case 4096: return launch_spectra_t<4096>(a, s);
+    case 8192: return launch_spectra_t<8192>(a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+bool supported_padded_size(int P) { return P >= kMinP && P <= kMaxP && (P & (P - 1)) == 0; }
+
+}  // namespace seismic

@@ -1,0 +1,119 @@
+"""Seeded synthetic seismic waveforms.
+
+The reference's own dataset (``events_eruption_v8.npy``, loaded by every driver,
+e.g. Correlation_in_OMP/test_c.py:27) is not distributed, so workloads are
+built from seeded generators with the shapes and value distributions of the
+five workloads this library is measured on:
+
+* ``ricker_catalog``  -- Ricker wavelets, centre frequency U(2, 10) Hz at
+  100 Hz sampling, onset jitter U(+-50) samples, amplitude log-uniform in
+  [0.1, 10], random polarity, white noise at SNR U(5, 20) dB.
+* ``family_catalog``  -- events grouped in families; each family shares a
+  band-limited (2-15 Hz) Gaussian-noise template with cosine tapers of up to
+  400 samples; members are time-shifted U(+-100) samples, amplitude-scaled,
+  polarity-flipped, perturbed by 10 % independent band-limited noise and
+  buried in white noise at SNR U(0, 20) dB.
+
+All arrays are float32, shaped (N, C, L).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+FS_HZ = 100.0
+
+
+def ricker_catalog(n_events: int, length: int, seed: int = 1, n_channels: int = 1) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    t = (np.arange(length) - length / 2.0) / FS_HZ
+    out = np.empty((n_events, n_channels, length), np.float32)
+    for e in range(n_events):
+        for c in range(n_channels):
+            f = rng.uniform(2.0, 10.0)
+            onset = rng.uniform(-50.0, 50.0) / FS_HZ
+            amp = 10.0 ** rng.uniform(-1.0, 1.0)
+            pol = 1.0 if rng.random() < 0.5 else -1.0
+            tt = t - onset
+            a = (np.pi * f * tt) ** 2
+            w = (1.0 - 2.0 * a) * np.exp(-a) * amp * pol
+            snr_db = rng.uniform(5.0, 20.0)
+            rms = np.sqrt(np.mean(w * w))
+            noise = rng.standard_normal(length) * rms / (10.0 ** (snr_db / 20.0))
+            out[e, c] = (w + noise).astype(np.float32)
+    return out
+
+
+def _bandpass_noise(rng, shape, length, lo=2.0, hi=15.0):
+    x = rng.standard_normal(tuple(shape) + (length,))
+    spec = np.fft.rfft(x, axis=-1)
+    f = np.fft.rfftfreq(length, d=1.0 / FS_HZ)
+    spec[..., (f < lo) | (f > hi)] = 0.0
+    y = np.fft.irfft(spec, n=length, axis=-1)
+    y /= np.sqrt(np.mean(y * y, axis=-1, keepdims=True)) + 1e-30
+    return y
+
+
+def _taper(length, width=400):
+    w = min(width, length // 4)
+    tap = np.ones(length)
+    if w > 0:
+        ramp = 0.5 - 0.5 * np.cos(np.pi * np.arange(w) / w)
+        tap[:w] = ramp
+        tap[length - w:] = ramp[::-1]
+    return tap
+
+
+def family_catalog(n_events: int, n_channels: int, length: int, n_families: int | None = None,
+                   seed: int = 2) -> np.ndarray:
+    """Family-based generator; ``n_families`` defaults to max(1, N // 32)."""
+    rng = np.random.default_rng(seed)
+    if n_families is None:
+        n_families = max(1, n_events // 32)
+    tap = _taper(length)
+    templates = _bandpass_noise(rng, (n_families, n_channels), length) * tap
+    fam = rng.integers(0, n_families, size=n_events)
+    shifts = rng.integers(-100, 101, size=n_events)
+    amp = 10.0 ** rng.uniform(-0.5, 0.5, size=n_events)
+    pol = np.where(rng.random(n_events) < 0.5, -1.0, 1.0)
+    snr_db = rng.uniform(0.0, 20.0, size=n_events)
+    out = np.empty((n_events, n_channels, length), np.float32)
+    block = 2048
+    for s in range(0, n_events, block):
+        e = np.arange(s, min(n_events, s + block))
+        base = templates[fam[e]]                                   # (B, C, L)
+        shifted = np.zeros_like(base)
+        for k, sh in enumerate(shifts[e]):
+            if sh >= 0:
+                shifted[k, :, sh:] = base[k, :, :length - sh]
+            else:
+                shifted[k, :, :length + sh] = base[k, :, -sh:]
+        pert = _bandpass_noise(rng, (e.size, n_channels), length) * tap
+        sig = shifted + 0.1 * pert
+        sig *= (amp[e] * pol[e])[:, None, None]
+        rms = np.sqrt(np.mean(sig * sig, axis=-1, keepdims=True))
+        noise = rng.standard_normal(sig.shape) * rms / (10.0 ** (snr_db[e] / 20.0))[:, None, None]
+        out[e] = (sig + noise).astype(np.float32)
+    return out
+
+
+WORKLOADS = {
+    # name: (description, builder kwargs)
+    "small": dict(kind="ricker", n_events=200, n_channels=1, length=512, shift=512, seed=11),
+    "scale": dict(kind="family", n_events=4096, n_channels=3, length=2048, shift=2048,
+                  n_families=32, seed=12),
+    "precision": dict(kind="family", n_events=16384, n_channels=1, length=1024, shift=128,
+                      n_families=128, seed=13),
+}
+
+
+def make_workload(name: str, n_events: int | None = None) -> tuple[np.ndarray, int]:
+    """Events (N, C, L) and lag half-window ``shift`` of a named workload;
+    ``n_events`` overrides N (for bounded samples and small test cases)."""
+    w = WORKLOADS[name]
+    n = n_events if n_events is not None else w["n_events"]
+    if w["kind"] == "ricker":
+        ev = ricker_catalog(n, w["length"], seed=w["seed"], n_channels=w["n_channels"])
+    else:
+        ev = family_catalog(n, w["n_channels"], w["length"],
+                            n_families=max(1, min(w["n_families"], n // 32 or 1)), seed=w["seed"])
+    return ev, w["shift"]

@@ -1,0 +1,172 @@
+"""GPU parity tests of the FP32 fused path, through the C ABI.
+
+Reference outputs come from the golden fixtures (the reference's own OMP
+source + wrapper), from the C restatement (pinned bit-exact to those
+fixtures by test_oracle.py) on larger seeded inputs, and from the FP64
+oracle.  Tolerances: see tolerances.py.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from oracle import oracle as O
+from seismic_gb300 import correlation_lib, synth, xcorr
+from tolerances import check_hist, check_pairs
+
+pytestmark = pytest.mark.gpu
+
+
+class _Trace:
+    def __init__(self, d):
+        self.data = d
+
+
+def _traces(ev):
+    out = np.empty(ev.shape[0], dtype=object)
+    for k in range(ev.shape[0]):
+        out[k] = _Trace(ev[k])
+    return out
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_dropin_cpp_matches_reference_golden(cuda_ok, name):
+    g = load_golden(name)
+    ev = g["events"]
+    n = ev.shape[0]
+    thr = float(g["threshold"])
+    nh = int(g["n_classes_hist"])
+    got = correlation_lib.compute_correlation(_traces(ev), int(g["shift"]), 4, 1, thr, nh)
+    i, j = O.triu_pairs(n)
+    r = O.fp64_xcorr(ev, int(g["shift"]), i, j, padded=int(g["padded"]))
+    check_pairs(got[:4], (g["xcm_pos"], g["xclags_pos"], g["xcm_neg"], g["xclags_neg"]), r, thr, label=name)
+    check_hist(got[4], got[5], g["max_hist"], g["min_hist"], r, nh)
+
+
+@pytest.mark.parametrize("name", ["ricker_n64_l512_full", "family_n48_l1024_s128", "ragged_n37_l300_s200"])
+def test_dropin_cuda_signature_matches_golden(cuda_ok, name):
+    g = load_golden(name)
+    ev = g["events"]
+    thr = float(g["threshold"])
+    correlation_lib.initialiseRunTime()
+    got = correlation_lib.compute_correlation_cuda(ev, int(g["shift"]), 8, thr)
+    i, j = O.triu_pairs(ev.shape[0])
+    r = O.fp64_xcorr(ev, int(g["shift"]), i, j, padded=int(g["padded"]))
+    check_pairs(got, (g["xcm_pos"], g["xclags_pos"], g["xcm_neg"], g["xclags_neg"]), r, thr, label=name)
+
+
+def test_small_workload_full_triangle_vs_port(cuda_ok):
+    """N=200 Ricker events, L=512, lags -511..512, full triangle."""
+    ev, shift = synth.make_workload("small")
+    ev = ev[:, 0]
+    exp = O.port_correlation_cpp(ev, shift, 0.0, 20)
+    got = correlation_lib.compute_correlation(ev, shift, 4, 4, 0.0, 20)
+    i, j = O.triu_pairs(ev.shape[0])
+    r = O.fp64_xcorr(ev, shift, i, j)
+    stats = check_pairs(got[:4], (exp.vals_pos, exp.lags_pos, exp.vals_neg, exp.lags_neg), r, 0.0)
+    check_hist(got[4], got[5], exp.max_hist, exp.min_hist, r, 20)
+    ag = O.agreement(*got[:4], r)
+    assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5
+    assert ag.lag_mismatch == 0, (ag, stats)
+
+
+@pytest.mark.parametrize("n,length,shift,thr,nh", [
+    (13, 2048, 2048, 0.0, 20),     # P = 4096, ragged tile
+    (9, 4096, 4096, 0.25, 10),     # P = 8192
+    (11, 32, 32, 0.0, 4),          # P = 64
+    (21, 200, 56, 0.1, 6),         # P = 256
+    (70, 700, 300, 0.05, 17),      # P = 1024, non-power-of-two L
+])
+def test_sizes_vs_port(cuda_ok, n, length, shift, thr, nh):
+    ev = synth.family_catalog(n, 1, length, n_families=max(1, n // 4), seed=n + length)[:, 0]
+    exp = O.port_correlation_cpp(ev, shift, thr, nh)
+    got = correlation_lib.compute_correlation(ev, shift, 2, 1, thr, nh)
+    i, j = O.triu_pairs(n)
+    r = O.fp64_xcorr(ev, shift, i, j)
+    check_pairs(got[:4], (exp.vals_pos, exp.lags_pos, exp.vals_neg, exp.lags_neg), r, thr)
+    check_hist(got[4], got[5], exp.max_hist, exp.min_hist, r, nh)
+
+
+def test_zero_norm_event_defined(cuda_ok):
+    ev = synth.ricker_catalog(6, 256, seed=31)[:, 0].copy()
+    ev[3] = 0.0
+    got = correlation_lib.compute_correlation(ev, 128, 1, 1, 0.0, 8)
+    exp = O.port_correlation_cpp(ev, 128, 0.0, 8)
+    np.testing.assert_array_equal(got[4], exp.max_hist)
+    np.testing.assert_array_equal(got[5], exp.min_hist)
+    idx = xcorr.packed_index(np.array([0, 1, 2, 3, 3, 3]), np.array([3, 3, 3, 3, 4, 5]), 6)
+    for a in got[:4]:
+        assert np.all(a[idx] == 0)
+
+
+def test_shift_zero_and_single_event(cuda_ok):
+    ev = synth.ricker_catalog(1, 100, seed=1)[:, 0]
+    got = correlation_lib.compute_correlation(ev, 50, 1, 1, 0.0, 4)
+    assert got[1][0] == 0 and abs(got[0][0] - 1.0) < 1e-5
+    ev = synth.ricker_catalog(5, 100, seed=2)[:, 0]
+    got = correlation_lib.compute_correlation(ev, 0, 1, 1, 0.0, 4)
+    for a in got[:4]:
+        assert np.all(a == 0)
+    assert got[4][0] == 15 and got[5][0] == 15   # every pair counted in bin 0
+
+
+def test_multichannel_vs_fp64(cuda_ok):
+    """3 channels, mean of per-channel normalised series, full lag range."""
+    ev = synth.family_catalog(40, 3, 1024, n_families=3, seed=41)
+    shift = 1024
+    res = xcorr.xcorr(ev, shift, threshold=0.0, n_classes_hist=20)
+    i, j = O.triu_pairs(40)
+    r = O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(1024, shift))
+    ag = O.agreement(res.vals_pos, res.lags_pos, res.vals_neg, res.lags_neg, r)
+    assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, ag
+    assert ag.lag_mismatch == 0, ag
+    assert res.max_hist.sum() == i.size and res.min_hist.sum() == i.size
+
+
+def test_device_api_torch_stream_and_workspace(cuda_ok):
+    import torch
+    from seismic_gb300 import _lib
+    ev = synth.family_catalog(50, 2, 600, n_families=2, seed=5)
+    t = torch.from_numpy(ev).cuda()
+    host = xcorr.xcorr(ev, 200, threshold=0.1, n_classes_hist=10)
+    lib = _lib.lib()
+    p = xcorr.resolve_padded_size(600, 200)
+    ws = torch.empty(lib.seismic_xcorr_workspace_bytes(50, 2, p, 0), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        dev = xcorr.xcorr(t, 200, threshold=0.1, n_classes_hist=10, workspace=ws)
+    s.synchronize()
+    np.testing.assert_array_equal(dev.vals_pos.cpu().numpy(), host.vals_pos)
+    np.testing.assert_array_equal(dev.lags_neg.cpu().numpy(), host.lags_neg)
+    np.testing.assert_array_equal(dev.max_hist.cpu().numpy(), host.max_hist)
+    small = torch.empty(16, dtype=torch.uint8, device="cuda")
+    with pytest.raises(_lib.SeismicError):
+        xcorr.xcorr(t, 200, workspace=small)
+
+
+def test_precision_workload_size_properties(cuda_ok):
+    """Full-size N=16384, L=1024, +-128 lags: properties that hold at any size
+    (diagonal coefficient 1 at lag 0, |coef| <= 1, histogram totals) and an
+    FP64 check of a random sample of pairs."""
+    import torch
+    ev, shift = synth.make_workload("precision")
+    n = ev.shape[0]
+    t = torch.from_numpy(ev).cuda()
+    res = xcorr.xcorr(t, shift, threshold=0.0, n_classes_hist=20)
+    vp = res.vals_pos.cpu().numpy()
+    lp = res.lags_pos.cpu().numpy()
+    vn = res.vals_neg.cpu().numpy()
+    ln = res.lags_neg.cpu().numpy()
+    diag = xcorr.packed_index(np.arange(n), np.arange(n), n)
+    assert np.abs(vp[diag] - 1.0).max() < 1e-5
+    assert np.all(lp[diag] == 0)
+    assert vp.max() <= 1.0 + 1e-5 and vn.min() >= -1.0 - 1e-5
+    assert int(res.max_hist.sum()) == vp.size and int(res.min_hist.sum()) == vp.size
+    rng = np.random.default_rng(0)
+    i = rng.integers(0, n, 3000)
+    j = rng.integers(0, n, 3000)
+    i, j = np.minimum(i, j), np.maximum(i, j)
+    idx = xcorr.packed_index(i, j, n)
+    r = O.fp64_xcorr(ev, shift, i, j)
+    ag = O.agreement(vp[idx], lp[idx], vn[idx], ln[idx], r)
+    assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, ag
+    assert ag.lag_mismatch == 0, ag

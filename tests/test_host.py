@@ -1,0 +1,110 @@
+"""CPU tests of the host-side logic: the C ABI library loads and exports every
+symbol the public header declares, host-only entry points, the Python
+drop-in's padding, and the pair scheduler's coverage of the triangle."""
+import ctypes
+import subprocess
+
+import numpy as np
+import pytest
+
+from seismic_gb300 import _lib, correlation_lib, xcorr
+
+
+def test_library_exports_every_header_symbol(built_lib):
+    names = _lib.header_symbols()
+    assert {"correlationCPP", "correlationCUDA", "initialiseCUDA"} <= set(names)
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    missing = [n for n in names if n not in exported]
+    assert not missing, f"declared in the header but not exported: {missing}"
+    for n in names:
+        assert hasattr(built_lib, n)
+
+
+def test_resolve_padded_size(built_lib):
+    assert xcorr.resolve_padded_size(512, 512) == 1024
+    assert xcorr.resolve_padded_size(1024, 128) == 2048
+    assert xcorr.resolve_padded_size(1000, 1000) == 2048
+    assert xcorr.resolve_padded_size(3000, 3000) == 8192
+    assert xcorr.resolve_padded_size(5000, 5000) == 0
+    assert xcorr.resolve_padded_size(10, 5) == 64
+
+
+def test_status_strings(built_lib):
+    assert built_lib.seismic_status_string(0) == b"ok"
+    assert built_lib.seismic_status_string(2) == b"unsupported size"
+
+
+def test_workspace_bytes(built_lib):
+    b = built_lib.seismic_xcorr_workspace_bytes(1000, 3, 2048, 0)
+    assert b >= 1000 * 3 * 1024 * 8 + 1000 * 3 * 8
+    assert built_lib.seismic_xcorr_workspace_bytes(1000, 3, 1000, 0) == 0
+
+
+def test_dropin_padding_matches_reference_rule():
+    class Tr:
+        def __init__(self, d):
+            self.data = d
+    rng = np.random.default_rng(0)
+    evs = np.empty(3, dtype=object)
+    for k, length in enumerate((300, 300, 250)):
+        evs[k] = Tr(rng.standard_normal(length).astype(np.float32))
+    n, length, p, padded, rev = correlation_lib._pad(evs)
+    assert (n, length, p) == (3, 300, 512)          # L from events[0], P = 1 << L.bit_length()
+    np.testing.assert_array_equal(padded[2, :250], evs[2].data)
+    assert np.all(padded[2, 250:] == 0)
+    np.testing.assert_array_equal(rev[0, :300], evs[0].data[::-1])
+
+
+def test_packed_index():
+    n = 7
+    i, j = np.triu_indices(n)
+    np.testing.assert_array_equal(xcorr.packed_index(i, j, n), np.arange(n * (n + 1) // 2))
+    big = 100_000
+    assert xcorr.packed_index(big - 1, big - 1, big) == big * (big + 1) // 2 - 1
+
+
+def _scheduler_pairs(n, tile):
+    """Python restatement of the pair kernel's work decomposition
+    (decode_tile + couple split in pairs.cu) to check coverage."""
+    nb = (n + tile - 1) // tile
+    cpt = tile * tile // 2
+    total = nb * (nb + 1) // 2 * cpt
+    seen = []
+    for w in range(total):
+        tl, lc = divmod(w, cpt)
+        twonb1 = 2.0 * nb + 1.0
+        b = int((twonb1 - np.sqrt(twonb1 * twonb1 - 8.0 * tl)) * 0.5)
+        b = min(max(b, 0), nb - 1)
+        start = lambda q: q * nb - q * (q - 1) // 2  # noqa: E731
+        while b + 1 < nb and start(b + 1) <= tl:
+            b += 1
+        while b > 0 and start(b) > tl:
+            b -= 1
+        bi, bj = b, b + (tl - start(b))
+        ii, jj = divmod(2 * lc, tile)
+        i = bi * tile + ii
+        for j in (bj * tile + jj, bj * tile + jj + 1):
+            if i < n and j < n and j >= i:
+                seen.append((i, j))
+    return seen
+
+
+@pytest.mark.parametrize("n,tile", [(1, 8), (2, 8), (13, 8), (37, 4), (64, 8), (9, 2), (50, 2)])
+def test_scheduler_covers_triangle_exactly_once(n, tile):
+    seen = _scheduler_pairs(n, tile)
+    assert len(seen) == len(set(seen)) == n * (n + 1) // 2
+
+
+def test_native_api_rejects_bad_sizes_without_gpu(built_lib):
+    """Argument validation runs before any CUDA call."""
+    st = built_lib.seismic_xcorr_host(ctypes.c_void_p(1), 4, 1, 100, 100, 100, 96, 10, 0.0, 0, 0,
+                                      ctypes.c_void_p(1), ctypes.c_void_p(1), ctypes.c_void_p(1),
+                                      ctypes.c_void_p(1), None, None)
+    assert st == 2  # unsupported padded size
+    assert b"unsupported" in built_lib.seismic_last_error_message()
+    st = built_lib.seismic_xcorr_host(ctypes.c_void_p(1), 0, 1, 100, 100, 100, 128, 10, 0.0, 0, 0,
+                                      ctypes.c_void_p(1), ctypes.c_void_p(1), ctypes.c_void_p(1),
+                                      ctypes.c_void_p(1), None, None)
+    assert st == 1

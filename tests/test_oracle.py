@@ -1,0 +1,122 @@
+"""CPU tests of the oracle: the FFTW-API shim, the C restatement (port)
+against the golden fixtures made by the reference itself, the port against
+the reference build where the reference tree exists, and analytic
+known-answer tests of the FP64 oracle."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, load_golden
+from oracle import oracle as O
+from seismic_gb300 import synth
+
+
+def test_golden_fixtures_present():
+    assert len(golden_cases()) >= 8
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_port_matches_reference_golden_bit_exact(name):
+    g = load_golden(name)
+    out = O.port_correlation_cpp(g["events"], int(g["shift"]), float(g["threshold"]),
+                                 int(g["n_classes_hist"]), num_threads=2, chunk_size=3)
+    np.testing.assert_array_equal(out.vals_pos, g["xcm_pos"])
+    np.testing.assert_array_equal(out.lags_pos, g["xclags_pos"])
+    np.testing.assert_array_equal(out.vals_neg, g["xcm_neg"])
+    np.testing.assert_array_equal(out.lags_neg, g["xclags_neg"])
+    np.testing.assert_array_equal(out.max_hist, g["max_hist"])
+    np.testing.assert_array_equal(out.min_hist, g["min_hist"])
+
+
+@pytest.mark.parametrize("name", golden_cases())
+def test_golden_against_fp64(name):
+    """The reference's own outputs sit within 1e-5 of the FP64 restatement."""
+    g = load_golden(name)
+    n = g["events"].shape[0]
+    i, j = O.triu_pairs(n)
+    r = O.fp64_xcorr(g["events"], int(g["shift"]), i, j, padded=int(g["padded"]))
+    ag = O.agreement(g["xcm_pos"], g["xclags_pos"], g["xcm_neg"], g["xclags_neg"], r,
+                     threshold=float(g["threshold"]))
+    assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, ag
+    near = (np.abs(r.val_pos - float(g["threshold"])) < 1e-5).sum()
+    assert ag.lag_mismatch <= near, ag
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/Correlation_in_OMP/correlation_c.cpp"),
+                    reason="reference tree not present")
+def test_port_matches_reference_build_random():
+    ev = synth.family_catalog(33, 1, 700, n_families=3, seed=77)[:, 0]
+    a = O.port_correlation_cpp(ev, 300, 0.1, 9)
+    b = O.ref_correlation_cpp(ev, 300, 0.1, 9)
+    for f in ("vals_pos", "lags_pos", "vals_neg", "lags_neg", "max_hist", "min_hist"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f))
+
+
+def test_port_close_to_fp64_config1_sample():
+    ev = synth.ricker_catalog(24, 512, seed=5)[:, 0]
+    out = O.port_correlation_cpp(ev, 512, 0.0, 20)
+    i, j = O.triu_pairs(24)
+    r = O.fp64_xcorr(ev, 512, i, j)
+    ag = O.agreement(out.vals_pos, out.lags_pos, out.vals_neg, out.lags_neg, r)
+    assert ag.max_err_pos < 5e-6 and ag.max_err_neg < 5e-6
+    assert ag.lag_mismatch == 0
+
+
+def test_fp64_kat_autocorrelation():
+    ev = synth.ricker_catalog(5, 256, seed=9)[:, 0]
+    i = np.arange(5)
+    r = O.fp64_xcorr(ev, 256, i, i)
+    np.testing.assert_allclose(r.val_pos, 1.0, atol=1e-12)
+    np.testing.assert_array_equal(r.lag_pos, 0)
+
+
+def test_fp64_kat_delay_sign():
+    """event 1 = event 0 delayed by d samples -> lag_pos of pair (0,1) is -d:
+    the series at lag d is sum_k x_0[k] x_1[k-d] (reference lag t+1 at
+    corr_t[L+t], Correlation_in_OMP/correlation_c.cpp:102-106)."""
+    rng = np.random.default_rng(3)
+    base = np.zeros(400)
+    base[100:200] = rng.standard_normal(100)
+    for d in (7, -13, 0, 150):
+        shifted = np.roll(base, d)
+        ev = np.stack([base, shifted]).astype(np.float32)
+        r = O.fp64_xcorr(ev, 256, np.array([0]), np.array([1]))
+        assert r.lag_pos[0] == -d
+        assert abs(r.val_pos[0] - 1.0) < 1e-6
+
+
+def test_fp64_kat_negated():
+    ev = synth.ricker_catalog(1, 300, seed=4)[:, 0]
+    pair = np.stack([ev[0], -ev[0]]).astype(np.float32)
+    r = O.fp64_xcorr(pair, 150, np.array([0]), np.array([1]))
+    assert abs(r.val_neg[0] + 1.0) < 1e-7 and r.lag_neg[0] == 0
+
+
+def test_fp64_multichannel_mean():
+    ev = synth.family_catalog(4, 3, 256, n_families=1, seed=8)
+    r3 = O.fp64_xcorr(ev, 64, np.array([0]), np.array([1]))
+    # mean of per-channel normalised series: bounded by 1, and == 1 for identical events
+    assert r3.val_pos[0] <= 1.0 + 1e-12
+    same = O.fp64_xcorr(np.stack([ev[0], ev[0]]), 64, np.array([0]), np.array([1]))
+    assert abs(same.val_pos[0] - 1.0) < 1e-12 and same.lag_pos[0] == 0
+
+
+def test_port_zero_event_defined():
+    """An all-zero event: the reference divides by zero and indexes its
+    histogram with int(NaN); the port counts NaN nowhere and outputs 0/0."""
+    ev = synth.ricker_catalog(4, 128, seed=2)[:, 0].copy()
+    ev[2] = 0
+    out = O.port_correlation_cpp(ev, 64, 0.0, 5)
+    idx = O.packed_index(np.array([0, 1, 2, 2]), np.array([2, 2, 2, 3]), 4)
+    assert np.all(out.lags_pos[idx] == 0)
+    assert out.max_hist.sum() == 10 - 4
+
+
+def test_hist_rule_matches_reference_port():
+    ev = synth.ricker_catalog(30, 512, seed=21)[:, 0]
+    out = O.port_correlation_cpp(ev, 512, 0.0, 13)
+    i, j = O.triu_pairs(30)
+    # with threshold 0 the reported values are the un-thresholded ones (> 0)
+    np.testing.assert_array_equal(O.hist_bins(out.vals_pos, 13, False), out.max_hist)
+    np.testing.assert_array_equal(O.hist_bins(out.vals_neg, 13, True), out.min_hist)
