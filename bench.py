@@ -168,6 +168,7 @@ def cpu_baseline(workload: str, ev: np.ndarray, shift: int, n_sample: int | None
                 fn(x, shift, 0.0, 20, num_threads=cores, chunk_size=4, padded=p)
             times.append(time.perf_counter() - t0)
     finally:
+        ctypes.CDLL(None).fflush(None)  # drain C stdio buffers while fd 1 is still /dev/null
         os.dup2(saved, 1)
         os.close(saved)
         os.close(devnull)
@@ -231,7 +232,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     lib = _lib.lib()
-    ev, shift = synth.make_workload(args.workload)
+    ev, shift = synth.make_workload(args.workload, n_events=args.n_events)
     if ws > 1:  # weak scaling: every rank its own catalog of the same shape
         ev = synth.family_catalog(ev.shape[0], ev.shape[1], ev.shape[2], seed=1000 + rank) \
             if args.workload != "small" else ev
@@ -395,6 +396,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOAD_TEXT), default="scale")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--n-events", type=int, default=None, help="override N (small profiling cases only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

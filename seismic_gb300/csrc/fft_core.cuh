@@ -145,21 +145,51 @@ template <int DIR> __device__ __forceinline__ float2 twiddle_lookup(const float2
 
 // v[r] *= w^r, r = 1..R-1, w = exp(DIR 2 pi i m / (NS R)); powers from one
 // table entry and a shallow product tree (at most 4 roundings per power).
+template <int R> __device__ __forceinline__ void apply_root_powers(float2 *v, float2 w1) {
+  float2 w[R];
+  w[1] = w1;
+#pragma unroll
+  for (int r = 2; r < R; ++r) w[r] = (r & 1) ? cmul(w[r - 1], w1) : cmul(w[r / 2], w[r / 2]);
+#pragma unroll
+  for (int r = 1; r < R; ++r) v[r] = cmul(v[r], w[r]);
+}
+
 template <int P, int R, int NS, int DIR>
 __device__ __forceinline__ void apply_twiddles(float2 *v, int m, const float2 *__restrict__ tw) {
   if constexpr (NS == 1) {
     return;
   } else {
     constexpr int step = kMaxP / (NS * R);
-    const float2 w1 = twiddle_lookup<DIR>(tw, m * step);
-    float2 w[R];
-    w[1] = w1;
-#pragma unroll
-    for (int r = 2; r < R; ++r) w[r] = (r & 1) ? cmul(w[r - 1], w1) : cmul(w[r / 2], w[r / 2]);
-#pragma unroll
-    for (int r = 1; r < R; ++r) v[r] = cmul(v[r], w[r]);
+    apply_root_powers<R>(v, twiddle_lookup<DIR>(tw, m * step));
   }
 }
+
+// Twiddle roots w1 = exp(DIR 2 pi i m / (NS R)) of every job of the radix-16
+// passes after the first.  They depend only on the thread index, so a
+// persistent kernel loads them once; passes of smaller radix look theirs up.
+template <int P, int DIR> struct TwiddleRoots {
+  using PL = FftPlan<P>;
+  static constexpr int G = P / 32;
+  static constexpr int NS2 = 16, NS3 = 16 * PL::R2, NS4 = 16 * PL::R2 * (PL::R3 ? PL::R3 : 1);
+  static constexpr bool H2 = PL::R2 == 16, H3 = PL::R3 == 16, H4 = PL::R4 == 16;
+  float2 w2[H2 ? 2 : 1], w3[H3 ? 2 : 1], w4[H4 ? 2 : 1];
+
+  __device__ __forceinline__ void load(int t, const float2 *__restrict__ tw) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int j = t + q * G;
+      if constexpr (H2) w2[q] = twiddle_lookup<DIR>(tw, (j % NS2) * (kMaxP / (NS2 * 16)));
+      if constexpr (H3) w3[q] = twiddle_lookup<DIR>(tw, (j % NS3) * (kMaxP / (NS3 * 16)));
+      if constexpr (H4) w4[q] = twiddle_lookup<DIR>(tw, (j % NS4) * (kMaxP / (NS4 * 16)));
+    }
+  }
+  // roots of pass `pass` (2, 3 or 4), or nullptr when that pass looks them up
+  template <int PASS> __device__ __forceinline__ const float2 *get() const {
+    if constexpr (PASS == 2) return H2 ? w2 : nullptr;
+    else if constexpr (PASS == 3) return H3 ? w3 : nullptr;
+    else return H4 ? w4 : nullptr;
+  }
+};
 
 // ------------------------------------------------------------- group sync
 // A group is G consecutive threads of a CTA.  Groups of <= 32 threads live in
@@ -198,13 +228,17 @@ template <int P, int R> __device__ __forceinline__ void pass_read(const float2 *
 }
 
 template <int P, int R, int NS, int DIR>
-__device__ __forceinline__ void pass_compute(float2 (&v)[32], int t, const float2 *__restrict__ tw) {
+__device__ __forceinline__ void pass_compute(float2 (&v)[32], int t, const float2 *__restrict__ tw,
+                                             const float2 *roots = nullptr) {
   constexpr int G = P / 32;
   constexpr int J = 32 / R;
 #pragma unroll
   for (int q = 0; q < J; ++q) {
     const int j = t + q * G;
-    apply_twiddles<P, R, NS, DIR>(&v[q * R], j % NS, tw);
+    if (roots != nullptr)
+      apply_root_powers<R>(&v[q * R], roots[q]);
+    else
+      apply_twiddles<P, R, NS, DIR>(&v[q * R], j % NS, tw);
     dft<R, DIR>(&v[q * R]);
   }
 }

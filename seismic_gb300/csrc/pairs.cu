@@ -38,10 +38,11 @@ __host__ __device__ __forceinline__ long long tri_start(long long b, long long n
   return b * nb - b * (b - 1) / 2;
 }
 
-// Row-major decode of tile index x over the upper triangle of nb x nb tiles.
+// Row-major decode of tile index x over the upper triangle of nb x nb tiles:
+// a single-precision estimate of the row, corrected exactly in integers.
 __device__ __forceinline__ void decode_tile(long long x, long long nb, long long &bi, long long &bj) {
-  const double twonb1 = 2.0 * (double)nb + 1.0;
-  long long b = (long long)((twonb1 - sqrt(twonb1 * twonb1 - 8.0 * (double)x)) * 0.5);
+  const float twonb1 = 2.0f * (float)nb + 1.0f;
+  long long b = (long long)((twonb1 - sqrtf(fmaxf(twonb1 * twonb1 - 8.0f * (float)x, 0.f))) * 0.5f);
   if (b < 0) b = 0;
   if (b > nb - 1) b = nb - 1;
   while (b + 1 < nb && tri_start(b + 1, nb) <= x) ++b;
@@ -61,18 +62,6 @@ int pair_tile_for(int P) { return P <= 2048 ? 8 : (P == 4096 ? 4 : 2); }
 __device__ __forceinline__ void cmac_conj(float2 &y, float2 a, float2 b) {
   y.x = fmaf(a.x, b.x, fmaf(a.y, b.y, y.x));
   y.y = fmaf(a.y, b.x, fmaf(-a.x, b.y, y.y));
-}
-
-struct Best {
-  float v;  // value (>= 0 for max, <= 0 for min)
-  int d;    // lag, INT_MIN while v == 0
-};
-
-__device__ __forceinline__ void upd_max(Best &b, float v, int d) {
-  if (v > b.v || (v == b.v && d < b.d)) { b.v = v; b.d = d; }
-}
-__device__ __forceinline__ void upd_min(Best &b, float v, int d) {
-  if (v < b.v || (v == b.v && d < b.d)) { b.v = v; b.d = d; }
 }
 
 __device__ __forceinline__ int hist_bin(float v, float delta, int n_hist) {
@@ -114,7 +103,12 @@ __global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
   const long long cpt = T * T / 2;
   const long long stride = (long long)gridDim.x * NG;
   const int d0 = 1 - a.shift;
+  const bool full_window = 2LL * a.shift >= P;  // every index m is inside the lag window
+  const int span = full_window ? P : 2 * a.shift - 1;  // inside iff (m - d0) mod P <= span
   const unsigned gmask = group_lane_mask<G>();
+  // Twiddle roots of the radix-16 passes depend only on the thread: load once.
+  TwiddleRoots<P, 1> roots;
+  roots.load(t, a.twiddles);
 
   const int ca = (t == 0) ? 0 : t;
   const int cb = (t == 0) ? S / 2 : S - t;
@@ -201,71 +195,99 @@ __global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
     group_sync<G>(g);
     pass_read<P, PL::R2>(buf, v, t);
     group_sync<G>(g);
-    pass_compute<P, PL::R2, 16, 1>(v, t, a.twiddles);
+    pass_compute<P, PL::R2, 16, 1>(v, t, a.twiddles, roots.template get<2>());
     if constexpr (PL::R3 != 0) {
       pass_write<P, PL::R2, 16>(buf, v, t);
       group_sync<G>(g);
       pass_read<P, PL::R3>(buf, v, t);
       group_sync<G>(g);
-      pass_compute<P, PL::R3, 16 * PL::R2, 1>(v, t, a.twiddles);
+      pass_compute<P, PL::R3, 16 * PL::R2, 1>(v, t, a.twiddles, roots.template get<3>());
       if constexpr (PL::R4 != 0) {
         pass_write<P, PL::R3, 16 * PL::R2>(buf, v, t);
         group_sync<G>(g);
         pass_read<P, PL::R4>(buf, v, t);
         group_sync<G>(g);
-        pass_compute<P, PL::R4, 16 * PL::R2 * PL::R3, 1>(v, t, a.twiddles);
+        pass_compute<P, PL::R4, 16 * PL::R2 * PL::R3, 1>(v, t, a.twiddles, roots.template get<4>());
       }
     }
 
-    // ---- window scan straight from the last pass's registers
-    Best pa{0.f, INT_MIN}, na{0.f, INT_MIN}, pb{0.f, INT_MIN}, nb2{0.f, INT_MIN};
+    // ---- window scan, phase A: per-thread max / min of both series.
+    //      Values outside the lag window are zeroed (0 never wins: only a
+    //      strictly positive maximum / strictly negative minimum counts).
 #pragma unroll
     for (int q = 0; q < 32 / RL; ++q) {
 #pragma unroll
       for (int r = 0; r < RL; ++r) {
-        const int m = last_pass_index<P, RL>(t, q, r);
-        const int d = d0 + ((m - d0) & (P - 1));
-        if (d <= a.shift) {
-          const float2 z = v[q * RL + r];
-          upd_max(pa, z.x, d);
-          upd_min(na, z.x, d);
-          upd_max(pb, z.y, d);
-          upd_min(nb2, z.y, d);
+        if (!full_window) {
+          const int m = last_pass_index<P, RL>(t, q, r);
+          if (((m - d0) & (P - 1)) > span) v[q * RL + r] = make_float2(0.f, 0.f);
         }
       }
     }
-
-    // ---- group argmax / argmin: value by redux.max on the float bits
-    //      (all candidates are >= 0), then the smallest lag among the winners
-    unsigned key[4] = {__float_as_uint(pa.v), __float_as_uint(fabsf(na.v)), __float_as_uint(pb.v),
-                       __float_as_uint(fabsf(nb2.v))};
-    int lag[4] = {pa.d, na.d, pb.d, nb2.d};
+    float mx0 = 0.f, mn0 = 0.f, mx1 = 0.f, mn1 = 0.f;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const unsigned kmax = __reduce_max_sync(gmask, key[k]);
-      lag[k] = __reduce_min_sync(gmask, key[k] == kmax ? lag[k] : INT_MAX);
-      key[k] = kmax;
+    for (int e = 0; e < 32; ++e) {
+      mx0 = fmaxf(mx0, v[e].x);
+      mn0 = fminf(mn0, v[e].x);
+      mx1 = fmaxf(mx1, v[e].y);
+      mn1 = fminf(mn1, v[e].y);
     }
+    // ---- phase B: group maxima of the four magnitudes (float bits of values
+    //      >= 0 order like unsigned integers)
+    const unsigned own[4] = {__float_as_uint(mx0), __float_as_uint(-mn0) & 0x7fffffffu, __float_as_uint(mx1),
+                             __float_as_uint(-mn1) & 0x7fffffffu};
+    unsigned key[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) key[k] = __reduce_max_sync(gmask, own[k]);
     if constexpr (NW > 1) {
       if ((t & 31) == 0) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          red[(t >> 5) * 8 + k] = key[k];
-          red[(t >> 5) * 8 + 4 + k] = (unsigned)lag[k];
+        for (int k = 0; k < 4; ++k) red[(t >> 5) * 8 + k] = key[k];
+      }
+      group_sync<G>(g);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        unsigned mk = red[k];
+#pragma unroll
+        for (int wv = 1; wv < NW; ++wv) mk = max(mk, red[wv * 8 + k]);
+        key[k] = mk;
+      }
+    }
+    // ---- phase C: threads holding a winning value find its smallest lag
+    //      (first occurrence in increasing lag, as the reference's scan)
+    int lag[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
+    const bool owner = (key[0] && own[0] == key[0]) || (key[1] && own[1] == key[1]) ||
+                       (key[2] && own[2] == key[2]) || (key[3] && own[3] == key[3]);
+    if (owner) {
+#pragma unroll
+      for (int q = 0; q < 32 / RL; ++q) {
+#pragma unroll
+        for (int r = 0; r < RL; ++r) {
+          const int m = last_pass_index<P, RL>(t, q, r);
+          const int d = d0 + ((m - d0) & (P - 1));
+          const float2 z = v[q * RL + r];
+          if (__float_as_uint(z.x) == key[0]) lag[0] = min(lag[0], d);
+          if (__float_as_uint(-z.x) == key[1]) lag[1] = min(lag[1], d);
+          if (__float_as_uint(z.y) == key[2]) lag[2] = min(lag[2], d);
+          if (__float_as_uint(-z.y) == key[3]) lag[3] = min(lag[3], d);
         }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) lag[k] = __reduce_min_sync(gmask, lag[k]);
+    if constexpr (NW > 1) {
+      if ((t & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) red[(t >> 5) * 8 + 4 + k] = (unsigned)lag[k];
       }
       group_sync<G>(g);
       if (t == 0) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          for (int wv = 1; wv < NW; ++wv) {
-            const unsigned kk = red[wv * 8 + k];
-            const int ll = (int)red[wv * 8 + 4 + k];
-            if (kk > key[k] || (kk == key[k] && ll < lag[k])) { key[k] = kk; lag[k] = ll; }
-          }
+#pragma unroll
+          for (int wv = 0; wv < NW; ++wv) lag[k] = min(lag[k], (int)red[wv * 8 + 4 + k]);
         }
       }
-      group_sync<G>(g);
     }
 
     // ---- epilogue: normalise (FP64), histogram, threshold, packed write

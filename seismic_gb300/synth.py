@@ -72,7 +72,7 @@ def family_catalog(n_events: int, n_channels: int, length: int, n_families: int 
     tap = _taper(length)
     templates = _bandpass_noise(rng, (n_families, n_channels), length) * tap
     fam = rng.integers(0, n_families, size=n_events)
-    shifts = rng.integers(-100, 101, size=n_events)
+    shifts = np.clip(rng.integers(-100, 101, size=n_events), -(length // 2), length // 2)
     amp = 10.0 ** rng.uniform(-0.5, 0.5, size=n_events)
     pol = np.where(rng.random(n_events) < 0.5, -1.0, 1.0)
     snr_db = rng.uniform(0.0, 20.0, size=n_events)
