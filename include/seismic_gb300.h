@@ -143,6 +143,32 @@ int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long
                          int form, float *d_vals_pos, int *d_lags_pos, float *d_vals_neg, int *d_lags_neg,
                          int *d_max_hist, int *d_min_hist, void *stream);
 
+/* seismic_xcorr_device for callers that cannot allocate device memory.
+ * No counterpart in the reference: it exists for callers that must not call
+ * cudaMalloc/cudaFree -- a host framework that has reserved nearly all of
+ * the GPU's memory for its own pool, a process under a fixed device-memory
+ * quota, or a latency-critical loop that cannot afford an allocation's
+ * implicit synchronisation.  Arguments and results are those of
+ * seismic_xcorr_device (FP32 form, no workspace argument); the scratch for
+ * the spectra and norms is one fixed array of seismic_noalloc_scratch_bytes()
+ * (64 MiB) inside this library, reserved on every device that uses it until
+ * the process exits.  Catalogs needing more than that
+ * (n_events*n_channels*(padded_size*4 + 8) bytes, 256-byte rounded per part)
+ * are rejected with SEISMIC_ERR_WORKSPACE_TOO_SMALL.  The first call on a
+ * device sets that device up, so make it before any stream capture.  All
+ * calls share the scratch: calls that overlap on the GPU (other streams or
+ * threads) race and must be serialised by the caller.  The call allocates
+ * nothing: no cudaMalloc, no cudaFree, no allocating library routine. */
+int seismic_xcorr_device_noalloc(const float *d_events, long long n_events, int n_channels, int event_length,
+                                 long long event_stride, long long channel_stride, int padded_size, int shift,
+                                 float threshold, int n_classes_hist, float *d_vals_pos, int *d_lags_pos,
+                                 float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist,
+                                 void *stream);
+
+/* Size in bytes of the fixed scratch used by seismic_xcorr_device_noalloc.
+ * No counterpart in the reference. */
+size_t seismic_noalloc_scratch_bytes(void);
+
 /* Number of kernels this library has launched in this process. */
 unsigned long long seismic_launch_count(void);
 

@@ -59,6 +59,10 @@ def _declare(lib):
         "seismic_pairs_device": (ctypes.c_int, [vp, vp, c_ll, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_int,
                                                 vp, vp, vp, vp, vp, vp, vp]),
+        "seismic_xcorr_device_noalloc": (ctypes.c_int, [vp, c_ll, ctypes.c_int, ctypes.c_int, c_ll, c_ll,
+                                                        ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                        ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]),
+        "seismic_noalloc_scratch_bytes": (ctypes.c_size_t, []),
         "seismic_launch_count": (ctypes.c_ulonglong, []),
         "seismic_release_cached_memory": (ctypes.c_int, []),
     }

@@ -184,6 +184,15 @@ static int run_pairs(const DeviceState &st, const float2 *spectra, const double 
   return SEISMIC_OK;
 }
 
+// Used by entry points defined in other translation units.
+int report_status(int status, const char *message) { return set_status(status, "%s", message); }
+int report_cuda(cudaError_t e, const char *what) { return cuda_status(e, what); }
+void note_launches(unsigned n) { g_launches.fetch_add(n); }
+int check_xcorr_args(long long n_events, int n_channels, int event_length, int padded, int shift, int n_hist,
+                     int form) {
+  return validate(n_events, n_channels, event_length, padded, shift, n_hist, form);
+}
+
 // Core: spectra + pairs on `stream`; buffers all on device.
 static int run_xcorr(const DeviceState &st, const float *d_events, long long n, int C, int L, long long ev_stride,
                      long long ch_stride, int P, int shift, float thr, int n_hist, float *vp, int *lp, float *vn,

@@ -66,4 +66,12 @@ const float2 *twiddle_table();
 
 bool supported_padded_size(int P);
 
+// Status plumbing shared by the entry points of every translation unit
+// (defined in api.cu): set the calling thread's status / message.
+int report_status(int status, const char *message);
+int report_cuda(cudaError_t e, const char *what);
+void note_launches(unsigned n);
+int check_xcorr_args(long long n_events, int n_channels, int event_length, int padded, int shift, int n_hist,
+                     int form);
+
 }  // namespace seismic
