@@ -254,14 +254,30 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
     sh = ctypes.c_void_p(stream.cuda_stream)
 
-    def spectra_call():
-        _lib.check(lib.seismic_spectra_device(d_ev.data_ptr(), n, c, length, c * length, length, p, prescale,
-                                              spectra.data_ptr(), norms.data_ptr(), sh))
+    form_code = _lib.FORMS[args.form]
+    if args.form == "fp32":
+        def spectra_call():
+            _lib.check(lib.seismic_spectra_device(d_ev.data_ptr(), n, c, length, c * length, length, p, prescale,
+                                                  spectra.data_ptr(), norms.data_ptr(), sh))
 
-    def pairs_call():
-        _lib.check(lib.seismic_pairs_device(spectra.data_ptr(), norms.data_ptr(), n, c, p, prescale, shift, 0.0, 20,
-                                            0, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(), ln.data_ptr(),
-                                            hist[0].data_ptr(), hist[1].data_ptr(), sh))
+        def pairs_call():
+            _lib.check(lib.seismic_pairs_device(spectra.data_ptr(), norms.data_ptr(), n, c, p, prescale, shift, 0.0,
+                                                20, 0, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(), ln.data_ptr(),
+                                                hist[0].data_ptr(), hist[1].data_ptr(), sh))
+    else:
+        wsb = lib.seismic_xcorr_workspace_bytes(n, c, length, shift, 0, form_code)
+        if wsb == 0:
+            raise SystemExit(f"form {args.form} does not support this workload")
+        lag_ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+
+        def spectra_call():  # the lag-GEMM form has no separate spectra step
+            return None
+
+        def pairs_call():
+            _lib.check(lib.seismic_xcorr_device(d_ev.data_ptr(), n, c, length, c * length, length, 0, shift, 0.0, 20,
+                                                form_code, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(),
+                                                ln.data_ptr(), hist[0].data_ptr(), hist[1].data_ptr(),
+                                                lag_ws.data_ptr(), wsb, sh))
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -320,7 +336,8 @@ def run_ours(args):
         h_hist = [np.zeros(20, np.int32), np.zeros(20, np.int32)]
 
         def host_call():
-            _lib.check(lib.seismic_xcorr_host(h_ev.data_ptr(), n, c, length, c * length, length, p, shift, 0.0, 20, 0,
+            _lib.check(lib.seismic_xcorr_host(h_ev.data_ptr(), n, c, length, c * length, length,
+                                              p if args.form == "fp32" else 0, shift, 0.0, 20, form_code,
                                               *(t.data_ptr() for t in h_out), h_hist[0].ctypes.data,
                                               h_hist[1].ctypes.data))
         torch.cuda.set_device(dev)
@@ -340,32 +357,49 @@ def run_ours(args):
                "d2h_bytes_per_step": int(4 * 4 * npairs + 2 * 20 * 4),
                "entry_point": "seismic_xcorr_host (C ABI), pinned host buffers, wall clock per call"}
 
-    # ---- roofline of the dominant kernel (pair kernel: FP32 pipe)
-    flops = npairs * fft_flops_per_pair(p, c)
+    # ---- roofline of the dominant kernel
     t_pair_mean = float(t_pair.mean())
-    achieved_tf = flops / t_pair_mean / 1e12
-    sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
-    sm_mhz = clk.get("sm_mhz") or 2070.0
-    peak_tf = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
-    traffic_pp = read_traffic(args.workload)
-    roofline = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
-                "frac": achieved_tf / peak_tf,
-                "traffic": (traffic_pp * npairs) if traffic_pp is not None else None,
-                "kernel": "pair_kernel",
-                "peak_source": f"nominal FP32 FMA rate: {sm_count} SMs x 128 lanes x 2 flop x median SM clock "
-                               f"{sm_mhz:.0f} MHz under load (MEASURED_PEAKS.json has no FP32 figure)",
-                "work": f"{npairs} pairs x (2.5 P log2 P + 6 C (P/2+1)) flop, P={p}, C={c}",
-                "pair_kernel_ms": t_pair_mean * 1e3, "pair_kernel_share_of_step": t_pair_mean / step_mean}
-    spec_bytes = rows * (length * 4 + (p // 2) * 8 + 8)
-    spectra_roof = {"bound": "hbm", "achieved": spec_bytes / float(t_spec.mean()) / 1e9, "unit": "GB/s",
-                    "ms": float(t_spec.mean()) * 1e3, "bytes": int(spec_bytes)}
+    traffic_pp = read_traffic(args.workload + ("" if args.form == "fp32" else "/" + args.form))
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        spectra_roof["peak"] = peaks["hbm_gbs"]
-        spectra_roof["frac"] = spectra_roof["achieved"] / peaks["hbm_gbs"]
-    except (OSError, KeyError, ValueError):
-        spectra_roof["peak"] = 6800.0
-        spectra_roof["peak_source"] = "fallback"
+    except (OSError, ValueError):
+        peaks = {}
+    if args.form == "fp32":  # pair kernel: FP32 pipe
+        flops = npairs * fft_flops_per_pair(p, c)
+        achieved_tf = flops / t_pair_mean / 1e12
+        sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
+        sm_mhz = clk.get("sm_mhz") or 2070.0
+        peak_tf = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roofline = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                    "frac": achieved_tf / peak_tf,
+                    "traffic": (traffic_pp * npairs) if traffic_pp is not None else None,
+                    "kernel": "pair_kernel",
+                    "peak_source": f"nominal FP32 FMA rate: {sm_count} SMs x 128 lanes x 2 flop x median SM clock "
+                                   f"{sm_mhz:.0f} MHz under load (MEASURED_PEAKS.json has no FP32 figure)",
+                    "work": f"{npairs} pairs x (2.5 P log2 P + 6 C (P/2+1)) flop, P={p}, C={c}",
+                    "pair_kernel_ms": t_pair_mean * 1e3, "pair_kernel_share_of_step": t_pair_mean / step_mean}
+    else:  # lag-GEMM: tensor pipe; algorithmic work 2 L (2 shift) per channel-pair, hi/lo extras not counted
+        flops = npairs * c * 2.0 * length * (2 * shift)
+        achieved_tf = flops / t_pair_mean / 1e12
+        peak_tf = peaks.get("bf16_tflops", 1900.0)
+        roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                    "frac": achieved_tf / peak_tf,
+                    "traffic": (traffic_pp * npairs) if traffic_pp is not None else None,
+                    "kernel": "lag_gemm_kernel (+ lag_prep_kernel, < 1 % of the step)",
+                    "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) of measured" if "bf16_tflops" in peaks
+                    else "fallback 1.9 PFLOP/s",
+                    "work": f"{npairs} pairs x {c} ch x 2 L (2 shift) flop, L={length}, shift={shift}; the three "
+                            f"BF16 hi/lo products issue 3x this on the tensor pipe",
+                    "pair_kernel_ms": t_pair_mean * 1e3, "pair_kernel_share_of_step": t_pair_mean / step_mean}
+    spec_bytes = rows * (length * 4 + (p // 2) * 8 + 8)
+    spectra_roof = None
+    if args.form == "fp32":
+        spectra_roof = {"bound": "hbm", "achieved": spec_bytes / float(t_spec.mean()) / 1e9, "unit": "GB/s",
+                        "ms": float(t_spec.mean()) * 1e3, "bytes": int(spec_bytes)}
+        spectra_roof["peak"] = peaks.get("hbm_gbs", 6800.0)
+        spectra_roof["frac"] = spectra_roof["achieved"] / spectra_roof["peak"]
+        if "hbm_gbs" not in peaks:
+            spectra_roof["peak_source"] = "fallback"
 
     out = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_mean * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -373,7 +407,7 @@ def run_ours(args):
            "data": "synthetic: seeded family-based waveforms (no public dataset; the reference's is not distributed)",
            "config": {"workload": args.workload + ": " + WORKLOAD_TEXT[args.workload], "n_events": n,
                       "n_channels": c, "event_length": length, "shift": shift, "padded_size": p,
-                      "pairs_per_step": npairs, "form": "fp32",
+                      "pairs_per_step": npairs, "form": args.form,
                       "l2": "L2 flushed (256 MB write) between timed steps; spectra > L2 for this workload"
                       if rows * p * 4 > 129e6 else "L2 flushed (256 MB write) between timed steps"},
            "fp64_error": fp64, "roofline": roofline, "spectra_kernel": spectra_roof, "e2e": e2e,
@@ -395,6 +429,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOAD_TEXT), default="scale")
+    ap.add_argument("--form", choices=["fp32", "laggemm"], default="fp32",
+                    help="fp32: fused FFT form; laggemm: tensor-core lag-GEMM (short windows)")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--n-events", type=int, default=None, help="override N (small profiling cases only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

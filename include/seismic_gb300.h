@@ -61,6 +61,14 @@ extern "C" {
 
 /* ---- computation forms -------------------------------------------------- */
 #define SEISMIC_FORM_FP32 0 /* FP32 spectra, FP32 products, FP32 inverse FFT */
+/* Time-domain lag sums on the tensor cores (tcgen05), BF16 hi+lo split with
+ * three products (hi*hi + hi*lo + lo*hi) accumulated in FP32; linear
+ * correlation (padded_size is not used); needs 2*shift <= 512 and the
+ * per-event lag strip to fit in shared memory (event_length up to ~1500 at
+ * 2*shift = 256). */
+#define SEISMIC_FORM_LAGGEMM_BF16X3 2
+
+#define SEISMIC_ERR_DEVICE_TIMEOUT 7 /* a kernel's bounded wait ran out; results invalid */
 
 /* ---- drop-in symbols (reference ABI) ----------------------------------- */
 
@@ -97,8 +105,16 @@ const char *seismic_status_string(int status);
  * maximum (8192). */
 int seismic_resolve_padded_size(int event_length, int shift);
 
-/* Device workspace (bytes) seismic_xcorr_device needs for these sizes. */
-size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int padded_size, int form);
+/* Device workspace (bytes) seismic_xcorr_device needs for these sizes
+ * (padded_size 0 = seismic_resolve_padded_size); 0 if the sizes are
+ * unsupported for the form. */
+size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int event_length, int shift,
+                                     int padded_size, int form);
+
+/* Returns SEISMIC_OK, or SEISMIC_ERR_DEVICE_TIMEOUT if a kernel of this
+ * library gave up a bounded wait since the last check (and clears the flag).
+ * Synchronises the current device. */
+int seismic_check_device_error(void);
 
 /* All-pairs correlation of device-resident events.
  *   d_events: element (e, c, s) at d_events[e*event_stride + c*channel_stride + s],

@@ -239,7 +239,8 @@ class Agreement:
     mean_err: float
     lag_mismatch: int          # mismatches that are NOT exempt
     lag_exempt: int            # mismatches exempt by the top-two-peaks rule
-    lag_agree_frac: float
+    lag_agree_frac: float      # raw agreement over all max and min lags
+    lag_agree_frac_untied: float = 1.0  # agreement where the FP64 extremum is unique (gap > 1e-9)
 
     def as_dict(self):
         return dict(self.__dict__)
@@ -270,6 +271,10 @@ def agreement(vals_pos, lags_pos, vals_neg, lags_neg, ref: Fp64Result, gap_tol: 
     n = vp.size
     bad = int((mis_p & ~ex_p).sum() + (mis_n & ~ex_n).sum())
     agree = 1.0 - (mis_p.sum() + mis_n.sum()) / max(1, 2 * n)
+    untied_p = ref.gap_pos > 1e-9
+    untied_n = ref.gap_neg > 1e-9
+    n_untied = int(untied_p.sum() + untied_n.sum())
+    agree_untied = 1.0 - ((mis_p & untied_p).sum() + (mis_n & untied_n).sum()) / max(1, n_untied)
     return Agreement(n, float(ep.max(initial=0.0)), float(en.max(initial=0.0)),
                      float(np.concatenate([ep, en]).mean()) if n else 0.0, bad,
-                     int(ex_p.sum() + ex_n.sum()), float(agree))
+                     int(ex_p.sum() + ex_n.sum()), float(agree), float(agree_untied))

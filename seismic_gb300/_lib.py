@@ -19,7 +19,7 @@ c_int_p = ctypes.POINTER(ctypes.c_int)
 c_ll = ctypes.c_longlong
 
 SEISMIC_OK = 0
-FORMS = {"fp32": 0}
+FORMS = {"fp32": 0, "laggemm": 2}
 
 _lib = None
 
@@ -45,8 +45,9 @@ def _declare(lib):
         "seismic_last_error_message": (ctypes.c_char_p, []),
         "seismic_status_string": (ctypes.c_char_p, [ctypes.c_int]),
         "seismic_resolve_padded_size": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
-        "seismic_xcorr_workspace_bytes": (ctypes.c_size_t, [c_ll, ctypes.c_int, ctypes.c_int,
-                                                            ctypes.c_int]),
+        "seismic_xcorr_workspace_bytes": (ctypes.c_size_t, [c_ll, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                            ctypes.c_int, ctypes.c_int]),
+        "seismic_check_device_error": (ctypes.c_int, []),
         "seismic_xcorr_device": (ctypes.c_int, [vp, c_ll, ctypes.c_int, ctypes.c_int, c_ll, c_ll,
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                 ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp,

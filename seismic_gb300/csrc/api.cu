@@ -61,6 +61,7 @@ struct DeviceState {
   bool ready = false;
   int sm_count = 0;
   const float2 *twiddles = nullptr;
+  int *error_flag = nullptr;  // set by kernels whose bounded waits ran out
   cudaStream_t stream = nullptr;
   // grow-only cached buffers used when the caller passes none
   void *ws = nullptr;
@@ -87,6 +88,8 @@ static int ensure_device(int *dev_out, DeviceState **st_out) {
     SEISMIC_TRY(cudaStreamSynchronize(st.stream), "twiddle init sync");
     st.twiddles = twiddle_table();
     if (!st.twiddles) return set_status(SEISMIC_ERR_CUDA, "twiddle table address");
+    st.error_flag = device_error_flag();
+    if (!st.error_flag) return set_status(SEISMIC_ERR_CUDA, "device error flag address");
     st.ready = true;
   }
   *dev_out = dev;
@@ -122,7 +125,16 @@ static int validate(long long n_events, int n_channels, int event_length, int pa
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "event_length %d exceeds paddedSize %d", event_length, padded);
   if (shift < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "shift must be >= 0");
   if (n_hist < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_classes_hist must be >= 0");
-  if (form != SEISMIC_FORM_FP32) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "unknown form %d", form);
+  if (form != SEISMIC_FORM_FP32 && form != SEISMIC_FORM_LAGGEMM_BF16X3)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "unknown form %d", form);
+  if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
+    if (shift < 1 || 2 * shift > 512)
+      return set_status(SEISMIC_ERR_UNSUPPORTED_SIZE, "lag-GEMM form needs 1 <= shift <= 256 (got %d)", shift);
+    if (!lag_plan(n_events, n_channels, event_length, shift, n_hist).ok)
+      return set_status(SEISMIC_ERR_UNSUPPORTED_SIZE,
+                        "lag-GEMM form: event_length %d with shift %d does not fit in shared memory", event_length,
+                        shift);
+  }
   // lag indices must fit in int32 alongside the sentinel values
   if (shift > (1 << 29)) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "shift too large");
   return SEISMIC_OK;
@@ -196,7 +208,15 @@ int check_xcorr_args(long long n_events, int n_channels, int event_length, int p
 // Core: spectra + pairs on `stream`; buffers all on device.
 static int run_xcorr(const DeviceState &st, const float *d_events, long long n, int C, int L, long long ev_stride,
                      long long ch_stride, int P, int shift, float thr, int n_hist, float *vp, int *lp, float *vn,
-                     int *ln, int *hmax, int *hmin, void *ws, cudaStream_t stream) {
+                     int *ln, int *hmax, int *hmin, void *ws, cudaStream_t stream, int form = SEISMIC_FORM_FP32) {
+  if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
+    int launched = 0;
+    cudaError_t e = launch_lag_gemm(d_events, n, C, L, ev_stride, ch_stride, shift, thr, n_hist, vp, lp, vn, ln,
+                                    hmax, hmin, ws, st.error_flag, st.sm_count, stream, &launched);
+    g_launches.fetch_add(launched);
+    SEISMIC_TRY(e, "lag-GEMM launch");
+    return SEISMIC_OK;
+  }
   const long long rows = n * C;
   float2 *spectra = reinterpret_cast<float2 *>(ws);
   double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(ws) + spectra_bytes(rows, P));
@@ -224,6 +244,7 @@ const char *seismic_status_string(int status) {
     case SEISMIC_ERR_CUDA: return "CUDA error";
     case SEISMIC_ERR_NO_DEVICE: return "no CUDA device";
     case SEISMIC_ERR_WORKSPACE_TOO_SMALL: return "workspace too small";
+    case SEISMIC_ERR_DEVICE_TIMEOUT: return "device wait timed out";
     default: return "unknown status";
   }
 }
@@ -238,11 +259,34 @@ int seismic_resolve_padded_size(int event_length, int shift) {
   return p <= kMaxP ? (int)p : 0;
 }
 
-size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int padded_size, int form) {
-  (void)form;
-  if (n_events < 1 || n_channels < 1 || !supported_padded_size(padded_size)) return 0;
+size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int event_length, int shift,
+                                     int padded_size, int form) {
+  if (n_events < 1 || n_channels < 1 || event_length < 1) return 0;
+  if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
+    if (!lag_plan(n_events, n_channels, event_length, shift, 0).ok) return 0;
+    return lag_workspace_bytes(n_events, n_channels, event_length);
+  }
+  if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  if (!supported_padded_size(padded_size)) return 0;
   const long long rows = n_events * n_channels;
   return spectra_bytes(rows, padded_size) + norms_bytes(rows);
+}
+
+int seismic_check_device_error(void) {
+  set_status(SEISMIC_OK, "");
+  int dev;
+  DeviceState *st;
+  int s = ensure_device(&dev, &st);
+  if (s) return s;
+  SEISMIC_TRY(cudaDeviceSynchronize(), "device synchronise");
+  int flag = 0;
+  SEISMIC_TRY(cudaMemcpy(&flag, st->error_flag, sizeof(int), cudaMemcpyDeviceToHost), "error flag read");
+  if (flag) {
+    const int zero = 0;
+    SEISMIC_TRY(cudaMemcpy(st->error_flag, &zero, sizeof(int), cudaMemcpyHostToDevice), "error flag clear");
+    return set_status(SEISMIC_ERR_DEVICE_TIMEOUT, "a kernel gave up a bounded wait; its results are invalid");
+  }
+  return SEISMIC_OK;
 }
 
 int seismic_xcorr_device(const float *d_events, long long n_events, int n_channels, int event_length,
@@ -261,7 +305,7 @@ int seismic_xcorr_device(const float *d_events, long long n_events, int n_channe
   int dev;
   DeviceState *st;
   if ((s = ensure_device(&dev, &st))) return s;
-  const size_t need = seismic_xcorr_workspace_bytes(n_events, n_channels, padded_size, form);
+  const size_t need = seismic_xcorr_workspace_bytes(n_events, n_channels, event_length, shift, padded_size, form);
   if (workspace) {
     if (workspace_bytes < need)
       return set_status(SEISMIC_ERR_WORKSPACE_TOO_SMALL, "workspace %zu < %zu bytes", workspace_bytes, need);
@@ -272,7 +316,7 @@ int seismic_xcorr_device(const float *d_events, long long n_events, int n_channe
   }
   return run_xcorr(*st, d_events, n_events, n_channels, event_length, event_stride, channel_stride, padded_size,
                    shift, threshold, n_classes_hist, d_vals_pos, d_lags_pos, d_vals_neg, d_lags_neg, d_max_hist,
-                   d_min_hist, workspace, (cudaStream_t)stream);
+                   d_min_hist, workspace, (cudaStream_t)stream, form);
 }
 
 int seismic_spectra_device(const float *d_events, long long n_events, int n_channels, int event_length,
@@ -334,7 +378,7 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
   const size_t ev_b = align256((size_t)rows * event_length * sizeof(float));
   const size_t out_b = align256((size_t)npairs * 4);
   const size_t hist_b = align256((size_t)2 * (n_classes_hist > 0 ? n_classes_hist : 1) * sizeof(int));
-  const size_t ws_b = seismic_xcorr_workspace_bytes(n_events, n_channels, padded_size, form);
+  const size_t ws_b = seismic_xcorr_workspace_bytes(n_events, n_channels, event_length, shift, padded_size, form);
   const size_t total = ev_b + 4 * out_b + hist_b + ws_b;
 
   std::lock_guard<std::mutex> lock(g_mutex);  // the cached io buffer is shared
@@ -357,7 +401,7 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
     SEISMIC_TRY(cudaMemsetAsync(d_hist, 0, 2 * (size_t)n_classes_hist * sizeof(int), stream), "hist clear");
   s = run_xcorr(*st, d_ev, n_events, n_channels, event_length, (long long)n_channels * event_length, event_length,
                 padded_size, shift, threshold, n_classes_hist, d_vp, d_lp, d_vn, d_ln, d_hist,
-                d_hist + (n_classes_hist > 0 ? n_classes_hist : 0), d_ws, stream);
+                d_hist + (n_classes_hist > 0 ? n_classes_hist : 0), d_ws, stream, form);
   if (s) return s;
   const size_t ob = (size_t)npairs * 4;
   SEISMIC_TRY(cudaMemcpyAsync(vals_pos, d_vp, ob, cudaMemcpyDeviceToHost, stream), "vals_pos D2H");
@@ -369,6 +413,15 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
     SEISMIC_TRY(cudaMemcpyAsync(h.data(), d_hist, h.size() * sizeof(int), cudaMemcpyDeviceToHost, stream),
                 "hist D2H");
   SEISMIC_TRY(cudaStreamSynchronize(stream), "host call sync");
+  if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
+    int flag = 0;
+    SEISMIC_TRY(cudaMemcpy(&flag, st->error_flag, sizeof(int), cudaMemcpyDeviceToHost), "error flag read");
+    if (flag) {
+      const int zero = 0;
+      cudaMemcpy(st->error_flag, &zero, sizeof(int), cudaMemcpyHostToDevice);
+      return set_status(SEISMIC_ERR_DEVICE_TIMEOUT, "lag-GEMM kernel gave up a bounded wait; results invalid");
+    }
+  }
   for (int k = 0; k < n_classes_hist; ++k) {
     max_hist[k] += h[k];
     min_hist[k] += h[n_classes_hist + k];

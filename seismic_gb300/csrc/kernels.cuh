@@ -66,6 +66,20 @@ const float2 *twiddle_table();
 
 bool supported_padded_size(int P);
 
+// ---- lag-GEMM form (laggemm.cu): time-domain lag sums on tcgen05 tensor cores
+struct LagPlan {
+  bool ok;
+  int lp, nt, wt, wpad, jp, nm, strip_bytes, xs_len, jc, stages, smem;
+};
+LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int n_hist);
+size_t lag_workspace_bytes(long long n_events, int n_channels, int length);
+cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length, long long ev_stride,
+                            long long ch_stride, int shift, float threshold, int n_hist, float *vp, int *lp,
+                            float *vn, int *ln, int *hmax, int *hmin, void *ws, int *error_flag, int sm_count,
+                            cudaStream_t s, int *launches);
+// Device address of the kernels' error flag (set when a bounded wait runs out).
+int *device_error_flag();
+
 // Status plumbing shared by the entry points of every translation unit
 // (defined in api.cu): set the calling thread's status / message.
 int report_status(int status, const char *message);

@@ -130,7 +130,7 @@ def test_device_api_torch_stream_and_workspace(cuda_ok):
     host = xcorr.xcorr(ev, 200, threshold=0.1, n_classes_hist=10)
     lib = _lib.lib()
     p = xcorr.resolve_padded_size(600, 200)
-    ws = torch.empty(lib.seismic_xcorr_workspace_bytes(50, 2, p, 0), dtype=torch.uint8, device="cuda")
+    ws = torch.empty(lib.seismic_xcorr_workspace_bytes(50, 2, 600, 200, p, 0), dtype=torch.uint8, device="cuda")
     s = torch.cuda.Stream()
     with torch.cuda.stream(s):
         dev = xcorr.xcorr(t, 200, threshold=0.1, n_classes_hist=10, workspace=ws)

@@ -37,9 +37,13 @@ def test_status_strings(built_lib):
 
 
 def test_workspace_bytes(built_lib):
-    b = built_lib.seismic_xcorr_workspace_bytes(1000, 3, 2048, 0)
+    b = built_lib.seismic_xcorr_workspace_bytes(1000, 3, 1024, 1024, 2048, 0)
     assert b >= 1000 * 3 * 1024 * 8 + 1000 * 3 * 8
-    assert built_lib.seismic_xcorr_workspace_bytes(1000, 3, 1000, 0) == 0
+    assert built_lib.seismic_xcorr_workspace_bytes(1000, 3, 1024, 1024, 1000, 0) == 0
+    # lag-GEMM form: two BF16 copies (hi, lo) of the events + FP64 norms
+    b = built_lib.seismic_xcorr_workspace_bytes(1000, 1, 1024, 128, 0, 2)
+    assert b >= 2 * 1000 * 1024 * 2 + 1000 * 8
+    assert built_lib.seismic_xcorr_workspace_bytes(1000, 1, 1024, 300, 0, 2) == 0  # 2*shift > 512
 
 
 def test_dropin_padding_matches_reference_rule():
