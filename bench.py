@@ -264,8 +264,8 @@ def run_ours(args):
             _lib.check(lib.seismic_pairs_device(spectra.data_ptr(), norms.data_ptr(), n, c, p, prescale, shift, 0.0,
                                                 20, 0, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(), ln.data_ptr(),
                                                 hist[0].data_ptr(), hist[1].data_ptr(), sh))
-    else:
-        wsb = lib.seismic_xcorr_workspace_bytes(n, c, length, shift, 0, form_code)
+    else:  # forms run as one call: spectra + pairs (fp16/bf16) or prep + lag-GEMM
+        wsb = lib.seismic_xcorr_workspace_bytes(n, c, length, shift, p if args.form != "laggemm" else 0, form_code)
         if wsb == 0:
             raise SystemExit(f"form {args.form} does not support this workload")
         lag_ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
@@ -274,7 +274,8 @@ def run_ours(args):
             return None
 
         def pairs_call():
-            _lib.check(lib.seismic_xcorr_device(d_ev.data_ptr(), n, c, length, c * length, length, 0, shift, 0.0, 20,
+            _lib.check(lib.seismic_xcorr_device(d_ev.data_ptr(), n, c, length, c * length, length,
+                                                p if args.form != "laggemm" else 0, shift, 0.0, 20,
                                                 form_code, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(),
                                                 ln.data_ptr(), hist[0].data_ptr(), hist[1].data_ptr(),
                                                 lag_ws.data_ptr(), wsb, sh))
@@ -364,7 +365,7 @@ def run_ours(args):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         peaks = {}
-    if args.form == "fp32":  # pair kernel: FP32 pipe
+    if args.form != "laggemm":  # FFT forms: pair kernel on the FP32 pipe
         flops = npairs * fft_flops_per_pair(p, c)
         achieved_tf = flops / t_pair_mean / 1e12
         sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -429,8 +430,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOAD_TEXT), default="scale")
-    ap.add_argument("--form", choices=["fp32", "laggemm"], default="fp32",
-                    help="fp32: fused FFT form; laggemm: tensor-core lag-GEMM (short windows)")
+    ap.add_argument("--form", choices=["fp32", "fp16", "bf16", "laggemm"], default="fp32",
+                    help="fp32: fused FFT form; fp16/bf16: half-precision spectra and products; "
+                         "laggemm: tensor-core lag-GEMM (short windows)")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--n-events", type=int, default=None, help="override N (small profiling cases only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

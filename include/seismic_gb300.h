@@ -61,6 +61,10 @@ extern "C" {
 
 /* ---- computation forms -------------------------------------------------- */
 #define SEISMIC_FORM_FP32 0 /* FP32 spectra, FP32 products, FP32 inverse FFT */
+/* FP16 (resp. BF16) spectra scaled by 1/norm, pointwise conj-products in
+ * FP16 (BF16) accumulated over channels in FP32, FP32 inverse FFT and scan. */
+#define SEISMIC_FORM_FP16_SPECTRA 1
+#define SEISMIC_FORM_BF16_SPECTRA 3
 /* Time-domain lag sums on the tensor cores (tcgen05), BF16 hi+lo split with
  * three products (hi*hi + hi*lo + lo*hi) accumulated in FP32; linear
  * correlation (padded_size is not used); needs 2*shift <= 512 and the

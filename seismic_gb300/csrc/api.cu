@@ -111,7 +111,13 @@ static int grow(void **ptr, size_t *have, size_t need, const char *what) {
 
 static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-static size_t spectra_bytes(long long rows, int P) { return align256((size_t)rows * (size_t)(P / 2) * sizeof(float2)); }
+// Spectrum storage of an FFT form: 0 float2, 1 half2, 2 bfloat162.
+static int form_stype(int form) {
+  return form == SEISMIC_FORM_FP16_SPECTRA ? 1 : (form == SEISMIC_FORM_BF16_SPECTRA ? 2 : 0);
+}
+static size_t spectra_bytes(long long rows, int P, int stype = 0) {
+  return align256((size_t)rows * (size_t)(P / 2) * (stype ? 4 : 8));
+}
 static size_t norms_bytes(long long rows) { return align256((size_t)rows * sizeof(double)); }
 
 static int validate(long long n_events, int n_channels, int event_length, int padded, int shift,
@@ -125,7 +131,8 @@ static int validate(long long n_events, int n_channels, int event_length, int pa
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "event_length %d exceeds paddedSize %d", event_length, padded);
   if (shift < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "shift must be >= 0");
   if (n_hist < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_classes_hist must be >= 0");
-  if (form != SEISMIC_FORM_FP32 && form != SEISMIC_FORM_LAGGEMM_BF16X3)
+  if (form != SEISMIC_FORM_FP32 && form != SEISMIC_FORM_LAGGEMM_BF16X3 && form != SEISMIC_FORM_FP16_SPECTRA &&
+      form != SEISMIC_FORM_BF16_SPECTRA)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "unknown form %d", form);
   if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
     if (shift < 1 || 2 * shift > 512)
@@ -141,9 +148,10 @@ static int validate(long long n_events, int n_channels, int event_length, int pa
 }
 
 static int run_spectra(const DeviceState &st, const float *d_events, long long n, int C, int L, long long ev_stride,
-                       long long ch_stride, int P, int prescale, float2 *spectra, double *norms,
-                       cudaStream_t stream) {
+                       long long ch_stride, int P, int prescale, void *spectra, double *norms, cudaStream_t stream,
+                       int stype = 0) {
   SpectraArgs sa;
+  sa.stype = stype;
   sa.events = d_events;
   sa.n_events = n;
   sa.n_channels = C;
@@ -159,11 +167,12 @@ static int run_spectra(const DeviceState &st, const float *d_events, long long n
   return SEISMIC_OK;
 }
 
-static int run_pairs(const DeviceState &st, const float2 *spectra, const double *norms, long long n, int C, int P,
+static int run_pairs(const DeviceState &st, const void *spectra, const double *norms, long long n, int C, int P,
                      int prescaled, int shift, float thr, int n_hist, float *vp, int *lp, float *vn, int *ln,
-                     int *hmax, int *hmin, cudaStream_t stream) {
+                     int *hmax, int *hmin, cudaStream_t stream, int stype = 0) {
   PairArgs pa;
   pa.spectra = spectra;
+  pa.stype = stype;
   pa.norms = norms;
   pa.n_events = n;
   pa.n_channels = C;
@@ -218,12 +227,15 @@ static int run_xcorr(const DeviceState &st, const float *d_events, long long n, 
     return SEISMIC_OK;
   }
   const long long rows = n * C;
-  float2 *spectra = reinterpret_cast<float2 *>(ws);
-  double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(ws) + spectra_bytes(rows, P));
-  const int prescale = C > 1 ? 1 : 0;
-  int s = run_spectra(st, d_events, n, C, L, ev_stride, ch_stride, P, prescale, spectra, norms, stream);
+  const int stype = form_stype(form);
+  void *spectra = ws;
+  double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(ws) + spectra_bytes(rows, P, stype));
+  // half-precision spectra are always scaled by 1/norm (keeps |X| <= sqrt(L))
+  const int prescale = (C > 1 || stype != 0) ? 1 : 0;
+  int s = run_spectra(st, d_events, n, C, L, ev_stride, ch_stride, P, prescale, spectra, norms, stream, stype);
   if (s) return s;
-  return run_pairs(st, spectra, norms, n, C, P, prescale, shift, thr, n_hist, vp, lp, vn, ln, hmax, hmin, stream);
+  return run_pairs(st, spectra, norms, n, C, P, prescale, shift, thr, n_hist, vp, lp, vn, ln, hmax, hmin, stream,
+                   stype);
 }
 
 }  // namespace seismic
@@ -269,7 +281,7 @@ size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int eve
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
   if (!supported_padded_size(padded_size)) return 0;
   const long long rows = n_events * n_channels;
-  return spectra_bytes(rows, padded_size) + norms_bytes(rows);
+  return spectra_bytes(rows, padded_size, form_stype(form)) + norms_bytes(rows);
 }
 
 int seismic_check_device_error(void) {
@@ -344,6 +356,8 @@ int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");
   if (n_classes_hist > 0 && (!d_max_hist || !d_min_hist))
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null histogram buffer");
+  if (form != SEISMIC_FORM_FP32)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "seismic_pairs_device pairs FP32 spectra (form 0)");
   if (n_channels > 1 && !prescaled)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "multichannel spectra must be prescaled");
   int dev;

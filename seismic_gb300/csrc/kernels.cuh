@@ -23,13 +23,15 @@ struct SpectraArgs {
   long long ev_stride;     // elements
   long long ch_stride;     // elements
   int prescale;            // 1: spectra scaled by 1/norm (0 if norm == 0); 0: unscaled
-  float2 *spectra;         // out [n_events*n_channels][P/2]
+  int stype;               // spectrum storage: 0 float2, 1 half2 (FP16), 2 bfloat162 (BF16)
+  void *spectra;           // out [n_events*n_channels][P/2] of stype
   double *norms;           // out [n_events*n_channels], FP64 L2 norms
   const float2 *twiddles;  // twiddle_table()
 };
 
 struct PairArgs {
-  const float2 *spectra;   // [n_events*n_channels][P/2]
+  const void *spectra;     // [n_events*n_channels][P/2] of stype
+  int stype;               // 0 float2, 1 half2, 2 bfloat162
   const double *norms;     // [n_events*n_channels]
   long long n_events;
   int n_channels;

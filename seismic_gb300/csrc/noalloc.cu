@@ -128,6 +128,7 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   sa.ev_stride = event_stride;
   sa.ch_stride = channel_stride;
   sa.prescale = prescale;
+  sa.stype = 0;  // FP32 spectra
   sa.spectra = spectra;
   sa.norms = norms;
   sa.twiddles = d->twiddles;
@@ -142,6 +143,7 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   pa.n_channels = n_channels;
   pa.shift = shift;
   pa.prescaled = prescale;
+  pa.stype = 0;
   pa.threshold = threshold;
   pa.n_hist = n_classes_hist;
   pa.delta_hist = n_classes_hist > 0 ? (float)(1.0 / n_classes_hist) : 0.f;

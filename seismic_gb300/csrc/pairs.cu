@@ -25,6 +25,9 @@
 // reporting lag t+1 (correlation_c.cpp:102-111); corr_t[L+t] equals the
 // circular correlation at d = t+1, so lag d is read at m = d mod P, and the
 // first-occurrence rule becomes "largest value, ties to the smallest d".
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include <climits>
 
 #include "fft_core.cuh"
@@ -58,11 +61,38 @@ long long pair_couples_total(long long n_events, int tile) {
 
 int pair_tile_for(int P) { return P <= 2048 ? 8 : (P == 4096 ? 4 : 2); }
 
-// Accumulate sum_c X_i conj X_j over channels: y += a * conj(b)
-__device__ __forceinline__ void cmac_conj(float2 &y, float2 a, float2 b) {
-  y.x = fmaf(a.x, b.x, fmaf(a.y, b.y, y.x));
-  y.y = fmaf(a.y, b.x, fmaf(-a.x, b.y, y.y));
-}
+// Spectrum storage types: 0 float2 (FP32 form), 1 half2, 2 bfloat162.  For
+// the half types the pointwise product a * conj(b) runs in the storage type
+// (HMUL2) and is accumulated over channels in FP32.
+template <int ST> struct SpecT;
+template <> struct SpecT<0> {
+  using T = float2;
+  __device__ static __forceinline__ void cmac_conj(float2 &y, float2 a, float2 b) {
+    y.x = fmaf(a.x, b.x, fmaf(a.y, b.y, y.x));
+    y.y = fmaf(a.y, b.x, fmaf(-a.x, b.y, y.y));
+  }
+  __device__ static __forceinline__ float2 f2(float2 a) { return a; }
+};
+template <> struct SpecT<1> {
+  using T = __half2;
+  __device__ static __forceinline__ void cmac_conj(float2 &y, __half2 a, __half2 b) {
+    const float2 p = __half22float2(__hmul2(a, b));                        // (ax bx, ay by)
+    const float2 q = __half22float2(__hmul2(a, __lowhigh2highlow(b)));     // (ax by, ay bx)
+    y.x += p.x + p.y;
+    y.y += q.y - q.x;
+  }
+  __device__ static __forceinline__ float2 f2(__half2 a) { return __half22float2(a); }
+};
+template <> struct SpecT<2> {
+  using T = __nv_bfloat162;
+  __device__ static __forceinline__ void cmac_conj(float2 &y, __nv_bfloat162 a, __nv_bfloat162 b) {
+    const float2 p = __bfloat1622float2(__hmul2(a, b));
+    const float2 q = __bfloat1622float2(__hmul2(a, __lowhigh2highlow(b)));
+    y.x += p.x + p.y;
+    y.y += q.y - q.x;
+  }
+  __device__ static __forceinline__ float2 f2(__nv_bfloat162 a) { return __bfloat1622float2(a); }
+};
 
 __device__ __forceinline__ int hist_bin(float v, float delta, int n_hist) {
   if (v >= 1.0f) return n_hist - 1;
@@ -70,8 +100,11 @@ __device__ __forceinline__ int hist_bin(float v, float delta, int n_hist) {
   return b > n_hist - 1 ? n_hist - 1 : (b < 0 ? 0 : b);
 }
 
-template <int P>
+template <int P, int ST>
 __global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
+  using SP = SpecT<ST>;
+  using ST_T = typename SP::T;
+  const ST_T *spectra = reinterpret_cast<const ST_T *>(a.spectra);
   constexpr int G = P / 32;
   constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
   constexpr int S = P / 16;
@@ -136,23 +169,24 @@ __global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
     }
     float dc1 = 0.f, dc2 = 0.f, nq1 = 0.f, nq2 = 0.f;
     for (int c = 0; c < C; ++c) {
-      const float2 *Xi = a.spectra + (i * C + c) * (long long)H;
-      const float2 *X1 = a.spectra + (ja * C + c) * (long long)H;
-      const float2 *X2 = a.spectra + (jb * C + c) * (long long)H;
+      const ST_T *Xi = spectra + (i * C + c) * (long long)H;
+      const ST_T *X1 = spectra + (ja * C + c) * (long long)H;
+      const ST_T *X2 = spectra + (jb * C + c) * (long long)H;
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
         const int ka = ca + r * S, kb = cb + r * S;
-        const float2 xa = __ldg(Xi + ka), pa = __ldg(X1 + ka), qa = __ldg(X2 + ka);
-        const float2 xb = __ldg(Xi + kb), pb = __ldg(X1 + kb), qb = __ldg(X2 + kb);
-        cmac_conj(ya1[r], xa, pa);
-        cmac_conj(ya2[r], xa, qa);
-        cmac_conj(yb1[r], xb, pb);
-        cmac_conj(yb2[r], xb, qb);
-        if (r == 0) {
-          dc1 = fmaf(xa.x, pa.x, dc1);
-          nq1 = fmaf(xa.y, pa.y, nq1);
-          dc2 = fmaf(xa.x, qa.x, dc2);
-          nq2 = fmaf(xa.y, qa.y, nq2);
+        const ST_T xa = __ldg(Xi + ka), pa = __ldg(X1 + ka), qa = __ldg(X2 + ka);
+        const ST_T xb = __ldg(Xi + kb), pb = __ldg(X1 + kb), qb = __ldg(X2 + kb);
+        SP::cmac_conj(ya1[r], xa, pa);
+        SP::cmac_conj(ya2[r], xa, qa);
+        SP::cmac_conj(yb1[r], xb, pb);
+        SP::cmac_conj(yb2[r], xb, qb);
+        if (r == 0) {  // slot 0 packs the two real bins DC and Nyquist
+          const float2 fx = SP::f2(xa), fp = SP::f2(pa), fq = SP::f2(qa);
+          dc1 = fmaf(fx.x, fp.x, dc1);
+          nq1 = fmaf(fx.y, fp.y, nq1);
+          dc2 = fmaf(fx.x, fq.x, dc2);
+          nq2 = fmaf(fx.y, fq.y, nq2);
         }
       }
     }
@@ -355,20 +389,29 @@ template <int P> static size_t pair_smem_bytes(int n_hist) {
   return s;
 }
 
-template <int P> static cudaError_t launch_pairs_t(const PairArgs &a, int grid, cudaStream_t s) {
+template <int P, int ST> static cudaError_t launch_pairs_st(const PairArgs &a, int grid, cudaStream_t s) {
   constexpr int G = P / 32;
   constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
   const size_t smem = pair_smem_bytes<P>(a.n_hist);
   static int configured_bytes = 0;
   if ((int)smem > configured_bytes) {
     const int want = (int)pair_smem_bytes<P>(kSmemHistMax);
-    cudaError_t e = cudaFuncSetAttribute(pair_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+    cudaError_t e = cudaFuncSetAttribute(pair_kernel<P, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
     if (e != cudaSuccess) return e;
     configured_bytes = want;
   }
   if (a.couple_end <= a.couple_begin) return cudaSuccess;
-  pair_kernel<P><<<grid, NG * G, smem, s>>>(a);
+  pair_kernel<P, ST><<<grid, NG * G, smem, s>>>(a);
   return cudaGetLastError();
+}
+
+template <int P> static cudaError_t launch_pairs_t(const PairArgs &a, int grid, cudaStream_t s) {
+  switch (a.stype) {
+    case 0: return launch_pairs_st<P, 0>(a, grid, s);
+    case 1: return launch_pairs_st<P, 1>(a, grid, s);
+    case 2: return launch_pairs_st<P, 2>(a, grid, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 template <int P> static int ctas_per_sm_t() {
@@ -376,9 +419,9 @@ template <int P> static int ctas_per_sm_t() {
   const size_t smem = pair_smem_bytes<P>(64);
   constexpr int G = P / 32;
   constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
-  cudaFuncSetAttribute(pair_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(pair_kernel<P, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)pair_smem_bytes<P>(kSmemHistMax));
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_kernel<P>, NG * G, smem) != cudaSuccess) n = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_kernel<P, 0>, NG * G, smem) != cudaSuccess) n = 1;
   return n > 0 ? n : 1;
 }
 

@@ -12,6 +12,9 @@
 // imaginary parts of one complex size-P FFT:
 //   z = a + i b,  Z = FFT(z),  A[k] = (Z[k] + conj Z[P-k]) / 2,
 //   B[k] = (Z[k] - conj Z[P-k]) / (2i).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
 #include "fft_core.cuh"
 #include "kernels.cuh"
 
@@ -38,6 +41,15 @@ const float2 *twiddle_table() {
   void *p = nullptr;
   if (cudaGetSymbolAddress(&p, g_twiddle) != cudaSuccess) return nullptr;
   return reinterpret_cast<const float2 *>(p);
+}
+
+__device__ __forceinline__ void store_spectrum(void *base, int stype, long long idx, float2 v) {
+  if (stype == 0)
+    reinterpret_cast<float2 *>(base)[idx] = v;
+  else if (stype == 1)
+    reinterpret_cast<__half2 *>(base)[idx] = __float22half2_rn(v);
+  else
+    reinterpret_cast<__nv_bfloat162 *>(base)[idx] = __float22bfloat162_rn(v);
 }
 
 template <int G> __device__ __forceinline__ double group_sum_double(double v, double *red, int g, int t) {
@@ -139,23 +151,25 @@ __global__ void __launch_bounds__(256) spectra_kernel(SpectraArgs a) {
     sa = na > 0.0 ? (float)(1.0 / na) : 0.f;
     sb = nb > 0.0 ? (float)(1.0 / nb) : 0.f;
   }
-  float2 *dst_a = a.spectra + row_a * (long long)H;
-  float2 *dst_b = a.spectra + row_b * (long long)H;
+  const long long off_a = row_a * (long long)H, off_b = row_b * (long long)H;
 #pragma unroll 4
   for (int k = t; k < H; k += G) {
     const float2 zk = buf[pad16(k)];
+    float2 va, vb;
     if (k == 0) {
       const float2 zh = buf[pad16(H)];
-      dst_a[0] = make_float2(zk.x * sa, zh.x * sa);
-      if (has_b) dst_b[0] = make_float2(zk.y * sb, zh.y * sb);
+      va = make_float2(zk.x * sa, zh.x * sa);
+      vb = make_float2(zk.y * sb, zh.y * sb);
     } else {
       const float2 zm = buf[pad16(P - k)];
       // A = (Z[k] + conj Z[P-k]) / 2 ; B = (Z[k] - conj Z[P-k]) / (2i)
       const float2 A = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
       const float2 B = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-      dst_a[k] = make_float2(A.x * sa, A.y * sa);
-      if (has_b) dst_b[k] = make_float2(B.x * sb, B.y * sb);
+      va = make_float2(A.x * sa, A.y * sa);
+      vb = make_float2(B.x * sb, B.y * sb);
     }
+    store_spectrum(a.spectra, a.stype, off_a + k, va);
+    if (has_b) store_spectrum(a.spectra, a.stype, off_b + k, vb);
   }
   if (t == 0) {
     a.norms[row_a] = na;
