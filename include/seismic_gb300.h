@@ -189,6 +189,57 @@ int seismic_xcorr_device_noalloc(const float *d_events, long long n_events, int 
  * No counterpart in the reference. */
 size_t seismic_noalloc_scratch_bytes(void);
 
+/* ---- batched form -------------------------------------------------------
+ * Many independent station catalogs (uneven N, L, channels) correlated by
+ * one persistent pair kernel (plus one spectra kernel) replayed from a
+ * captured CUDA graph.  No counterpart in the reference ABI, which handles
+ * one catalog per call (correlation_c.cpp:210); per catalog the semantics
+ * are those of seismic_xcorr_device in the FP32 form, at the padded size
+ * seismic_resolve_padded_size(event_length, shift). */
+typedef struct seismic_catalog {
+  const float *events; /* device; element (e, c, s) at e*event_stride + c*channel_stride + s */
+  long long n_events;
+  int n_channels;
+  int event_length;
+  long long event_stride;
+  long long channel_stride;
+  int shift;
+  float threshold;
+  int n_classes_hist; /* 0: no histograms */
+  float *vals_pos;    /* device outputs, n_events*(n_events+1)/2 each */
+  int *lags_pos;
+  float *vals_neg;
+  int *lags_neg;
+  int *max_hist; /* device int[n_classes_hist], accumulated into, or NULL */
+  int *min_hist;
+} seismic_catalog;
+
+typedef struct seismic_batch seismic_batch; /* opaque plan */
+
+#define SEISMIC_BATCH_NO_GRAPH 1 /* flag: launch directly instead of replaying a graph */
+
+/* Plans the batch (work lists sorted by cost, tuned tile sizes from the
+ * autotuner cache), allocates its workspace and captures the CUDA graph.
+ * The catalog buffers are bound to the plan; their contents may change
+ * between runs. */
+int seismic_batch_create(const seismic_catalog *catalogs, int n_catalogs, int flags, seismic_batch **out);
+/* Runs the whole batch on `stream` (asynchronous). */
+int seismic_batch_run(seismic_batch *batch, void *stream);
+int seismic_batch_destroy(seismic_batch *batch);
+/* Total pairs of all catalogs, kernels launched per run. */
+long long seismic_batch_pairs(const seismic_batch *batch);
+int seismic_batch_kernels_per_run(const seismic_batch *batch);
+
+/* ---- autotuner ---------------------------------------------------------
+ * Times the pair kernel for padded size P and n_channels over its tile
+ * sizes, CTAs per SM and batched item sizes on the current device and stores
+ * the fastest in the cache file (cache_path, else $SEISMIC_TUNE_CACHE, else
+ * ~/.cache/seismic_gb300/tune.txt).  Later plans of this process and of
+ * processes reading that file use it.  No counterpart in the reference. */
+int seismic_autotune(int padded_size, int n_channels, const char *cache_path);
+/* The parameters currently used for (P, n_channels). */
+int seismic_tuning(int padded_size, int n_channels, int *tile, int *ctas_per_sm, int *item_groups);
+
 /* Number of kernels this library has launched in this process. */
 unsigned long long seismic_launch_count(void);
 

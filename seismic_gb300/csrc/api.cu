@@ -187,21 +187,34 @@ static int run_pairs(const DeviceState &st, const void *spectra, const double *n
   pa.lags_neg = ln;
   pa.max_hist = hmax;
   pa.min_hist = hmin;
-  pa.tile = pair_tile_for(P);
+  const TuneEntry tune = tune_lookup(P, C);  // autotuner cache, else built-in defaults
+  pa.tile = tune.tile;
   pa.twiddles = st.twiddles;
   pa.couple_begin = 0;
   pa.couple_end = pair_couples_total(n, pa.tile);
   static int ctas_cache[16] = {0};
   const int lp2 = 31 - __builtin_clz((unsigned)P);
   if (!ctas_cache[lp2]) ctas_cache[lp2] = pair_ctas_per_sm(P);
+  const int ctas = (tune.ctas_per_sm > 0 && tune.ctas_per_sm < ctas_cache[lp2]) ? tune.ctas_per_sm : ctas_cache[lp2];
   const int G = P / 32;
   const int NG = (256 / G) > 0 ? (256 / G) : 1;
   long long want = (pa.couple_end + NG - 1) / NG;
-  long long grid = (long long)st.sm_count * ctas_cache[lp2];
+  long long grid = (long long)st.sm_count * ctas;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
   SEISMIC_TRY(launch_pairs(P, pa, (int)grid, stream), "pair kernel launch");
   g_launches.fetch_add(1);
+  return SEISMIC_OK;
+}
+
+int device_context(int *sm_count, const float2 **twiddles, int **error_flag) {
+  int dev;
+  DeviceState *st;
+  const int s = ensure_device(&dev, &st);
+  if (s) return s;
+  *sm_count = st->sm_count;
+  *twiddles = st->twiddles;
+  *error_flag = st->error_flag;
   return SEISMIC_OK;
 }
 

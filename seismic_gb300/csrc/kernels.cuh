@@ -68,6 +68,36 @@ const float2 *twiddle_table();
 
 bool supported_padded_size(int P);
 
+// ---- batched form: many independent catalogs in one persistent launch
+struct BatchCatalog {  // device-resident descriptor of one catalog
+  SpectraArgs spec;    // its events -> spectra, norms
+  PairArgs pairs;      // its spectra -> packed outputs (couple range unused)
+  int P;               // padded size of this catalog
+};
+struct BatchItem {     // a contiguous range of work of one catalog
+  int cat;
+  long long begin, end;  // spectra: row-pair indices; pairs: couple indices
+};
+cudaError_t launch_batched_spectra(const BatchCatalog *cats, const BatchItem *items, long long n_items, int grid,
+                                   cudaStream_t s);
+// Persistent pair launch over the items of the catalogs of one size P.
+cudaError_t launch_batched_pairs(int P, const BatchCatalog *cats, const BatchItem *items, long long n_items,
+                                 unsigned long long *counter, int grid, int max_hist, cudaStream_t s);
+// Also sets the kernel's shared-memory attribute: call before any capture.
+int batched_pairs_ctas_per_sm(int P, int max_hist);
+int groups_per_cta(int P);  // 256 / (P / 32), at least 1
+
+// Device context for entry points in other translation units (api.cu).
+int device_context(int *sm_count, const float2 **twiddles, int **error_flag);
+
+// ---- autotuner cache (autotune.cu): tuned pair-kernel parameters per (P, C)
+struct TuneEntry {
+  int tile;          // events per tile side
+  int ctas_per_sm;   // 0 = occupancy maximum
+  int item_groups;   // couples per batched work item, in units of groups per CTA
+};
+TuneEntry tune_lookup(int P, int n_channels);
+
 // ---- lag-GEMM form (laggemm.cu): time-domain lag sums on tcgen05 tensor cores
 struct LagPlan {
   bool ok;

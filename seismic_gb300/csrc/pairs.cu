@@ -101,7 +101,48 @@ __device__ __forceinline__ int hist_bin(float v, float delta, int n_hist) {
 }
 
 template <int P, int ST>
+__device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, long long w_stride, long long w_end,
+                                          unsigned char *smem_raw, int *hist, bool smem_hist);
+
+// Shared-memory layout of a 256-thread CTA working at size P: NG exchange
+// buffers, NG reduction slots, then the histogram (2 * n_hist ints).
+template <int P> __device__ __forceinline__ int *pair_hist_smem(unsigned char *smem_raw) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  constexpr int NW = (G + 31) / 32;
+  return reinterpret_cast<int *>(smem_raw + (size_t)NG * padded_len<P>() * sizeof(float2) +
+                                 (size_t)NG * NW * 8 * sizeof(unsigned));
+}
+
+template <int P, int ST>
 __global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
+  constexpr int NG = (256 / (P / 32)) > 0 ? (256 / (P / 32)) : 1;
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int *hist = pair_hist_smem<P>(smem_raw);
+  const bool smem_hist = a.n_hist > 0 && a.n_hist <= kSmemHistMax;
+  if (smem_hist) {
+    for (int h = threadIdx.x; h < 2 * a.n_hist; h += blockDim.x) hist[h] = 0;
+  }
+  __syncthreads();
+  const int g = threadIdx.x / (P / 32);
+  pair_body<P, ST>(a, a.couple_begin + (long long)blockIdx.x * NG + g, (long long)gridDim.x * NG, a.couple_end,
+                   smem_raw, hist, smem_hist);
+  if (smem_hist) {
+    __syncthreads();
+    for (int h = threadIdx.x; h < a.n_hist; h += blockDim.x) {
+      if (hist[h]) atomicAdd(&a.max_hist[h], hist[h]);
+      if (hist[a.n_hist + h]) atomicAdd(&a.min_hist[h], hist[a.n_hist + h]);
+    }
+  }
+}
+
+// Couples w = w_first, w_first + w_stride, ... < w_end of the triangle of
+// `a`, processed by this thread's group (G = P/32 threads).  `hist` is the
+// CTA's shared histogram (2 * n_hist ints) when smem_hist, else unused.
+template <int P, int ST>
+__device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, long long w_stride, long long w_end,
+                                          unsigned char *smem_raw, int *hist, bool smem_hist) {
   using SP = SpecT<ST>;
   using ST_T = typename SP::T;
   const ST_T *spectra = reinterpret_cast<const ST_T *>(a.spectra);
@@ -112,29 +153,18 @@ __global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
   constexpr int NW = (G + 31) / 32;
   using PL = FftPlan<P>;
   constexpr int RL = PL::R4 ? PL::R4 : (PL::R3 ? PL::R3 : PL::R2);
-
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *bufs = reinterpret_cast<float2 *>(smem_raw);
   unsigned *reds = reinterpret_cast<unsigned *>(bufs + NG * padded_len<P>());
-  int *hist = reinterpret_cast<int *>(reds + NG * NW * 8);
-
   const int g = threadIdx.x / G;
   const int t = threadIdx.x % G;
   float2 *buf = bufs + g * padded_len<P>();
   unsigned *red = reds + g * NW * 8;
-
-  const bool smem_hist = a.n_hist > 0 && a.n_hist <= kSmemHistMax;
-  if (smem_hist) {
-    for (int h = threadIdx.x; h < 2 * a.n_hist; h += blockDim.x) hist[h] = 0;
-  }
-  __syncthreads();
 
   const long long N = a.n_events;
   const int C = a.n_channels;
   const long long T = a.tile;
   const long long nb = (N + T - 1) / T;
   const long long cpt = T * T / 2;
-  const long long stride = (long long)gridDim.x * NG;
   const int d0 = 1 - a.shift;
   const bool full_window = 2LL * a.shift >= P;  // every index m is inside the lag window
   const int span = full_window ? P : 2 * a.shift - 1;  // inside iff (m - d0) mod P <= span
@@ -146,7 +176,7 @@ __global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
   const int ca = (t == 0) ? 0 : t;
   const int cb = (t == 0) ? S / 2 : S - t;
 
-  for (long long w = a.couple_begin + (long long)blockIdx.x * NG + g; w < a.couple_end; w += stride) {
+  for (long long w = w_first; w < w_end; w += w_stride) {
     const long long tile = w / cpt;
     const long long lc = w - tile * cpt;
     long long bi, bj;
@@ -370,15 +400,116 @@ __global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
       }
     }
   }
+}
 
+// ----------------------------------------------------------- batched form
+// One CTA-sized item of one catalog: the CTA's groups take its couples.
+template <int P>
+__device__ __forceinline__ void batched_pair_item(const PairArgs &a, long long begin, long long end,
+                                                  unsigned char *smem_raw) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  int *hist = pair_hist_smem<P>(smem_raw);
+  const bool smem_hist = a.n_hist > 0 && a.n_hist <= kSmemHistMax;
+  if (smem_hist)
+    for (int h = threadIdx.x; h < 2 * a.n_hist; h += blockDim.x) hist[h] = 0;
+  __syncthreads();
+  pair_body<P, 0>(a, begin + threadIdx.x / G, NG, end, smem_raw, hist, smem_hist);
+  __syncthreads();
   if (smem_hist) {
-    __syncthreads();
     for (int h = threadIdx.x; h < a.n_hist; h += blockDim.x) {
       if (hist[h]) atomicAdd(&a.max_hist[h], hist[h]);
       if (hist[a.n_hist + h]) atomicAdd(&a.min_hist[h], hist[a.n_hist + h]);
     }
   }
 }
+
+// Persistent over every catalog of transform size P: CTAs pull work items
+// from a global counter until the list is exhausted; items are pre-sorted by
+// cost (largest first).  One such launch per size present in a batch; the
+// batch graph runs them as concurrent branches.
+template <int P>
+__global__ void __launch_bounds__(256, 2)
+    batched_pair_kernel(const BatchCatalog *__restrict__ cats, const BatchItem *__restrict__ items, long long n_items,
+                        unsigned long long *counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long s_item;
+  __shared__ BatchItem s_w;
+  __shared__ __align__(16) PairArgs s_args;  // the item's catalog descriptor, read from shared memory
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = (long long)atomicAdd(counter, 1ULL);
+      if (s_item < n_items) {
+        s_w = items[s_item];
+        s_args = cats[s_w.cat].pairs;
+      }
+    }
+    __syncthreads();
+    const long long it = s_item;
+    if (it >= n_items) break;
+    batched_pair_item<P>(s_args, s_w.begin, s_w.end, smem_raw);
+    __syncthreads();  // s_item and the shared buffers are reused by the next item
+  }
+}
+
+template <int P> static size_t batched_pair_smem_t(int max_hist) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  constexpr int NW = (G + 31) / 32;
+  size_t s = (size_t)NG * padded_len<P>() * sizeof(float2) + (size_t)NG * NW * 8 * sizeof(unsigned);
+  if (max_hist > 0 && max_hist <= kSmemHistMax) s += (size_t)2 * max_hist * sizeof(int);
+  return s;
+}
+
+template <int P> static int batched_ctas_t(int max_hist) {
+  int n = 0;
+  cudaFuncSetAttribute(batched_pair_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)batched_pair_smem_t<P>(kSmemHistMax));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batched_pair_kernel<P>, 256,
+                                                    batched_pair_smem_t<P>(max_hist)) != cudaSuccess)
+    n = 1;
+  return n > 0 ? n : 1;
+}
+
+template <int P>
+static cudaError_t launch_batched_t(const BatchCatalog *cats, const BatchItem *items, long long n_items,
+                                    unsigned long long *counter, int grid, int max_hist, cudaStream_t s) {
+  // the shared-memory attribute was set by batched_pairs_ctas_per_sm during planning,
+  // so nothing but the launch happens here (it may be inside a stream capture)
+  batched_pair_kernel<P><<<grid, 256, batched_pair_smem_t<P>(max_hist), s>>>(cats, items, n_items, counter);
+  return cudaGetLastError();
+}
+
+int batched_pairs_ctas_per_sm(int P, int max_hist) {
+  switch (P) {
+    case 64: return batched_ctas_t<64>(max_hist);
+    case 128: return batched_ctas_t<128>(max_hist);
+    case 256: return batched_ctas_t<256>(max_hist);
+    case 512: return batched_ctas_t<512>(max_hist);
+    case 1024: return batched_ctas_t<1024>(max_hist);
+    case 2048: return batched_ctas_t<2048>(max_hist);
+    case 4096: return batched_ctas_t<4096>(max_hist);
+    case 8192: return batched_ctas_t<8192>(max_hist);
+    default: return 1;
+  }
+}
+
+cudaError_t launch_batched_pairs(int P, const BatchCatalog *cats, const BatchItem *items, long long n_items,
+                                 unsigned long long *counter, int grid, int max_hist, cudaStream_t s) {
+  switch (P) {
+    case 64: return launch_batched_t<64>(cats, items, n_items, counter, grid, max_hist, s);
+    case 128: return launch_batched_t<128>(cats, items, n_items, counter, grid, max_hist, s);
+    case 256: return launch_batched_t<256>(cats, items, n_items, counter, grid, max_hist, s);
+    case 512: return launch_batched_t<512>(cats, items, n_items, counter, grid, max_hist, s);
+    case 1024: return launch_batched_t<1024>(cats, items, n_items, counter, grid, max_hist, s);
+    case 2048: return launch_batched_t<2048>(cats, items, n_items, counter, grid, max_hist, s);
+    case 4096: return launch_batched_t<4096>(cats, items, n_items, counter, grid, max_hist, s);
+    case 8192: return launch_batched_t<8192>(cats, items, n_items, counter, grid, max_hist, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int groups_per_cta(int P) { return (256 / (P / 32)) > 0 ? (256 / (P / 32)) : 1; }
 
 template <int P> static size_t pair_smem_bytes(int n_hist) {
   constexpr int G = P / 32;

@@ -68,13 +68,24 @@ template <int G> __device__ __forceinline__ double group_sum_double(double v, do
   }
 }
 
+template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs &a, long long pair_index,
+                                                              unsigned char *smem_raw);
+
 template <int P>
 __global__ void __launch_bounds__(256) spectra_kernel(SpectraArgs a) {
   constexpr int G = P / 32;
   constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  spectra_body<P>(a, (long long)blockIdx.x * NG + threadIdx.x / G, smem_raw);
+}
+
+// Rows 2*pair_index and 2*pair_index+1 of `a`, by this thread's group.
+template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs &a, long long pair_index,
+                                                              unsigned char *smem_raw) {
+  constexpr int G = P / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
   constexpr int S = P / 16;
   constexpr int H = P / 2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *bufs = reinterpret_cast<float2 *>(smem_raw);
   double *reds = reinterpret_cast<double *>(bufs + NG * padded_len<P>());
 
@@ -84,7 +95,7 @@ __global__ void __launch_bounds__(256) spectra_kernel(SpectraArgs a) {
   double *red = reds + g * 2 * ((G + 31) / 32);
 
   const long long rows = a.n_events * (long long)a.n_channels;
-  const long long row_a = 2 * ((long long)blockIdx.x * NG + g);
+  const long long row_a = 2 * pair_index;
   if (row_a >= rows) return;  // whole group leaves together
   const long long row_b = row_a + 1;
   const bool has_b = row_b < rows;
@@ -193,6 +204,50 @@ template <int P> static cudaError_t launch_spectra_t(const SpectraArgs &a, cudaS
     configured = true;
   }
   spectra_kernel<P><<<(unsigned)ctas, NG * G, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+// Batched form: each item is up to one CTA's worth of row pairs (NG of its
+// size P) of one catalog; CTAs stride over the item list.
+__global__ void __launch_bounds__(256)
+    batched_spectra_kernel(const BatchCatalog *__restrict__ cats, const BatchItem *__restrict__ items,
+                           long long n_items) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const BatchItem w = items[it];
+    const SpectraArgs a = cats[w.cat].spec;
+    const int P = cats[w.cat].P;
+    const long long idx = w.begin + threadIdx.x / (P / 32);
+    if (idx < w.end) {
+      switch (P) {
+        case 64: spectra_body<64>(a, idx, smem_raw); break;
+        case 128: spectra_body<128>(a, idx, smem_raw); break;
+        case 256: spectra_body<256>(a, idx, smem_raw); break;
+        case 512: spectra_body<512>(a, idx, smem_raw); break;
+        case 1024: spectra_body<1024>(a, idx, smem_raw); break;
+        case 2048: spectra_body<2048>(a, idx, smem_raw); break;
+        case 4096: spectra_body<4096>(a, idx, smem_raw); break;
+        case 8192: spectra_body<8192>(a, idx, smem_raw); break;
+        default: break;
+      }
+    }
+    __syncthreads();  // the next item may lay its groups out differently
+  }
+}
+
+cudaError_t launch_batched_spectra(const BatchCatalog *cats, const BatchItem *items, long long n_items, int grid,
+                                   cudaStream_t s) {
+  // every size uses NG * (P + P/16) float2 = 69,632 bytes plus <= 2 KB of reduction slots
+  const size_t smem = (size_t)8 * (8192 + 512) + 2048;
+  static bool configured = false;  // first call happens before any capture (batch planning)
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(batched_spectra_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  if (n_items <= 0) return cudaSuccess;
+  batched_spectra_kernel<<<grid, 256, smem, s>>>(cats, items, n_items);
   return cudaGetLastError();
 }
 

@@ -77,22 +77,32 @@ def family_catalog(n_events: int, n_channels: int, length: int, n_families: int 
     pol = np.where(rng.random(n_events) < 0.5, -1.0, 1.0)
     snr_db = rng.uniform(0.0, 20.0, size=n_events)
     out = np.empty((n_events, n_channels, length), np.float32)
+    # 10 % waveform perturbation: band-limited traces drawn from a bank of
+    # 64 per catalog, each use with its own circular shift and sign
+    bank = (_bandpass_noise(rng, (min(64, n_events), n_channels), length) * tap).astype(np.float32)
+    bank2 = np.concatenate([bank, bank], axis=-1)                  # circular windows by slicing
+    windows = np.lib.stride_tricks.sliding_window_view(bank2, length, axis=-1)  # (K, C, 2L-?, L)
+    # templates shifted by s in [-L/2, L/2] with zero fill: slice a zero-padded copy
+    half = length // 2
+    tpad = np.zeros((n_families, n_channels, length + 2 * half), np.float32)
+    tpad[:, :, half:half + length] = templates
+    twin = np.lib.stride_tricks.sliding_window_view(tpad, length, axis=-1)     # (F, C, 2*half+1, L)
     block = 2048
     for s in range(0, n_events, block):
         e = np.arange(s, min(n_events, s + block))
-        base = templates[fam[e]]                                   # (B, C, L)
-        shifted = np.zeros_like(base)
-        for k, sh in enumerate(shifts[e]):
-            if sh >= 0:
-                shifted[k, :, sh:] = base[k, :, :length - sh]
-            else:
-                shifted[k, :, :length + sh] = base[k, :, -sh:]
-        pert = _bandpass_noise(rng, (e.size, n_channels), length) * tap
-        sig = shifted + 0.1 * pert
-        sig *= (amp[e] * pol[e])[:, None, None]
+        # event shifted right by sh: x[t] = template[t - sh]  ->  window starting at half - sh
+        shifted = twin[fam[e], :, half - shifts[e], :]                 # (B, C, L)
+        pick = rng.integers(0, bank.shape[0], size=e.size)
+        roll = rng.integers(0, length, size=e.size)
+        sign = np.where(rng.random(e.size) < 0.5, -1.0, 1.0).astype(np.float32)
+        pert = windows[pick, :, roll, :] * sign[:, None, None]
+        sig = shifted + np.float32(0.1) * pert
+        sig *= (amp[e] * pol[e]).astype(np.float32)[:, None, None]
         rms = np.sqrt(np.mean(sig * sig, axis=-1, keepdims=True))
-        noise = rng.standard_normal(sig.shape) * rms / (10.0 ** (snr_db[e] / 20.0))[:, None, None]
-        out[e] = (sig + noise).astype(np.float32)
+        scale = (rms / (10.0 ** (snr_db[e] / 20.0))[:, None, None]).astype(np.float32)
+        noise = rng.standard_normal(sig.shape, dtype=np.float32)
+        noise *= scale
+        out[e] = sig + noise
     return out
 
 
