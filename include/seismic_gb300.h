@@ -240,6 +240,41 @@ int seismic_autotune(int padded_size, int n_channels, const char *cache_path);
 /* The parameters currently used for (P, n_channels). */
 int seismic_tuning(int padded_size, int n_channels, int *tile, int *ctas_per_sm, int *item_groups);
 
+/* ---- serving loop --------------------------------------------------------
+ * A catalog kept resident on the device as packed half spectra (FP32 or
+ * FP16, form SEISMIC_FORM_FP32 / SEISMIC_FORM_FP16_SPECTRA) plus FP64 norms;
+ * query requests of up to max_query_events events are correlated against a
+ * contiguous catalog subset [subset_begin, subset_end) with continuous
+ * batching: requests are admitted in arrival order as soon as one of n_slots
+ * slots (CUDA streams) and enough of the hbm_budget_bytes pool are free
+ * (a request that does not fit lets later, smaller ones go first), and
+ * admitted requests run concurrently on the device.  No counterpart in the
+ * reference (which correlates one catalog with itself per call). */
+typedef struct seismic_server seismic_server;
+
+/* catalog: host float32 [n_catalog][n_channels][event_length].  hbm_budget
+ * 0 = room for n_slots requests of max_query_events against the whole
+ * catalog.  topk: matches reported per query event (0..64). */
+int seismic_server_create(const float *catalog, long long n_catalog, int n_channels, int event_length, int shift,
+                          float threshold, int form, int n_slots, size_t hbm_budget_bytes, int max_query_events,
+                          int topk, seismic_server **out);
+/* Enqueues a request and returns at once with a ticket.  query: host float32
+ * [n_query][n_channels][event_length], read when the request is admitted.
+ * Outputs (host, any may be NULL; pinned memory keeps the copies
+ * asynchronous): vals/lags [n_query][subset size] row-major, top-K values and
+ * catalog indices [n_query][topk] (largest max-coefficient, ties to the lower
+ * index).  All buffers must stay valid until seismic_server_wait returns. */
+int seismic_server_submit(seismic_server *server, const float *query, int n_query, long long subset_begin,
+                          long long subset_end, float *vals_pos, int *lags_pos, float *vals_neg, int *lags_neg,
+                          float *topk_vals, long long *topk_index, long long *ticket);
+/* Blocks until the ticket's results are in host memory; latency_ms (may be
+ * NULL) = submit -> completion. */
+int seismic_server_wait(seismic_server *server, long long ticket, double *latency_ms);
+int seismic_server_stats(seismic_server *server, long long *completed, long long *pairs, int *in_flight,
+                         int *pending);
+/* Waits for every admitted and pending request, then frees everything. */
+int seismic_server_destroy(seismic_server *server);
+
 /* Number of kernels this library has launched in this process. */
 unsigned long long seismic_launch_count(void);
 

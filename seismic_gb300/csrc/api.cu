@@ -150,7 +150,7 @@ static int validate(long long n_events, int n_channels, int event_length, int pa
 static int run_spectra(const DeviceState &st, const float *d_events, long long n, int C, int L, long long ev_stride,
                        long long ch_stride, int P, int prescale, void *spectra, double *norms, cudaStream_t stream,
                        int stype = 0) {
-  SpectraArgs sa;
+  SpectraArgs sa{};
   sa.stype = stype;
   sa.events = d_events;
   sa.n_events = n;
@@ -170,7 +170,7 @@ static int run_spectra(const DeviceState &st, const float *d_events, long long n
 static int run_pairs(const DeviceState &st, const void *spectra, const double *norms, long long n, int C, int P,
                      int prescaled, int shift, float thr, int n_hist, float *vp, int *lp, float *vn, int *ln,
                      int *hmax, int *hmin, cudaStream_t stream, int stype = 0) {
-  PairArgs pa;
+  PairArgs pa{};  // zero: triangle mode, no query spectra
   pa.spectra = spectra;
   pa.stype = stype;
   pa.norms = norms;

@@ -51,7 +51,21 @@ struct PairArgs {
   long long couple_end;
   int tile;                // events per tile side
   const float2 *twiddles;  // twiddle_table()
+  // Rectangle mode (rect != 0): pairs (query q, catalog event col_begin + j)
+  // for q < n_query, j < n_cols, instead of the upper triangle.  The query
+  // spectra / norms are separate; `spectra` / `norms` are the catalog's;
+  // outputs are [n_query][n_cols] row-major; couples are ordered in chunks of
+  // `tile` couple-columns times all queries (catalog spectra reused across
+  // queries from L1).
+  int rect;
+  const void *spectra_q;
+  const double *norms_q;
+  long long n_query;
+  long long col_begin;
+  long long n_cols;
 };
+// Couples covering a rectangle of n_query x n_cols pairs with chunk width `tile`.
+long long rect_couples_total(long long n_query, long long n_cols, int tile);
 
 // Number of two-pair work items ("couples") covering the upper triangle of
 // n_events with square tiles of `tile` events.

@@ -120,7 +120,7 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   double *norms = reinterpret_cast<double *>(d->scratch + spec_b);
   const int prescale = n_channels > 1 ? 1 : 0;
 
-  SpectraArgs sa;
+  SpectraArgs sa{};
   sa.events = d_events;
   sa.n_events = n_events;
   sa.n_channels = n_channels;
@@ -136,7 +136,7 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   if (e != cudaSuccess) return report_cuda(e, "spectra kernel launch");
   note_launches(1);
 
-  PairArgs pa;
+  PairArgs pa{};
   pa.spectra = spectra;
   pa.norms = norms;
   pa.n_events = n_events;

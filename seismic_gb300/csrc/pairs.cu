@@ -54,6 +54,12 @@ __device__ __forceinline__ void decode_tile(long long x, long long nb, long long
   bj = b + (x - tri_start(b, nb));
 }
 
+long long rect_couples_total(long long n_query, long long n_cols, int tile) {
+  const long long cols = (n_cols + 1) / 2;
+  const long long chunks = (cols + tile - 1) / tile;
+  return chunks * tile * n_query;
+}
+
 long long pair_couples_total(long long n_events, int tile) {
   const long long nb = (n_events + tile - 1) / tile;
   return nb * (nb + 1) / 2 * ((long long)tile * tile / 2);
@@ -176,20 +182,35 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
   const int ca = (t == 0) ? 0 : t;
   const int cb = (t == 0) ? S / 2 : S - t;
 
+  const ST_T *spectra_i = a.rect ? reinterpret_cast<const ST_T *>(a.spectra_q) : spectra;
   for (long long w = w_first; w < w_end; w += w_stride) {
-    const long long tile = w / cpt;
-    const long long lc = w - tile * cpt;
-    long long bi, bj;
-    decode_tile(tile, nb, bi, bj);
-    const long long ii = (2 * lc) / T, jj = (2 * lc) % T;
-    const long long i = bi * T + ii;
-    const long long j1 = bj * T + jj, j2 = j1 + 1;
-    const bool v1 = i < N && j1 < N && j1 >= i;
-    const bool v2 = i < N && j2 < N && j2 >= i;
-    if (!v1 && !v2) continue;  // uniform over the group
-    const long long ja = v1 ? j1 : j2;
-    const long long jb = j2 < N ? j2 : ja;
-    const bool out_b = v1 && v2;
+    long long i, ja, jb;
+    bool out_b;
+    if (!a.rect) {
+      const long long tile = w / cpt;
+      const long long lc = w - tile * cpt;
+      long long bi, bj;
+      decode_tile(tile, nb, bi, bj);
+      const long long ii = (2 * lc) / T, jj = (2 * lc) % T;
+      i = bi * T + ii;
+      const long long j1 = bj * T + jj, j2 = j1 + 1;
+      const bool v1 = i < N && j1 < N && j1 >= i;
+      const bool v2 = i < N && j2 < N && j2 >= i;
+      if (!v1 && !v2) continue;  // uniform over the group
+      ja = v1 ? j1 : j2;
+      jb = j2 < N ? j2 : ja;
+      out_b = v1 && v2;
+    } else {
+      // chunk of T couple-columns x all queries; j are subset columns
+      const long long per_chunk = a.n_query * T;
+      const long long chunk = w / per_chunk, r = w - chunk * per_chunk;
+      i = r / T;
+      const long long j1 = 2 * (chunk * T + (r - i * T)), j2 = j1 + 1;
+      if (j1 >= a.n_cols) continue;  // uniform over the group
+      out_b = j2 < a.n_cols;
+      ja = a.col_begin + j1;          // catalog event indices
+      jb = out_b ? ja + 1 : ja;
+    }
 
     // ---- conj products, accumulated over channels, for this thread's 16 bins
     float2 ya1[8], ya2[8], yb1[8], yb2[8];
@@ -199,7 +220,7 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
     }
     float dc1 = 0.f, dc2 = 0.f, nq1 = 0.f, nq2 = 0.f;
     for (int c = 0; c < C; ++c) {
-      const ST_T *Xi = spectra + (i * C + c) * (long long)H;
+      const ST_T *Xi = spectra_i + (i * C + c) * (long long)H;
       const ST_T *X1 = spectra + (ja * C + c) * (long long)H;
       const ST_T *X2 = spectra + (jb * C + c) * (long long)H;
 #pragma unroll
@@ -361,13 +382,14 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
         if (p == 1 && !out_b) break;
         const long long j = p == 0 ? ja : jb;
         const unsigned kp = key[2 * p], kn = key[2 * p + 1];
+        const double *norms_i = a.rect ? a.norms_q : a.norms;
         double denom;
         bool live = false;
         if (a.prescaled) {
-          for (int c = 0; c < C; ++c) live |= (a.norms[i * C + c] > 0.0) && (a.norms[j * C + c] > 0.0);
+          for (int c = 0; c < C; ++c) live |= (norms_i[i * C + c] > 0.0) && (a.norms[j * C + c] > 0.0);
           denom = (double)P * (double)C;
         } else {
-          const double ni = a.norms[i * C], nj = a.norms[j * C];
+          const double ni = norms_i[i * C], nj = a.norms[j * C];
           live = ni > 0.0 && nj > 0.0;
           denom = (double)P * ni * nj;
         }
@@ -392,7 +414,7 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
           if (!(vp > a.threshold)) { vp = 0.f; lp = 0; }
           if (!(vn < -a.threshold)) { vn = 0.f; ln = 0; }
         }
-        const long long idx = i * N - i * (i - 1) / 2 + (j - i);
+        const long long idx = a.rect ? i * a.n_cols + (j - a.col_begin) : i * N - i * (i - 1) / 2 + (j - i);
         a.vals_pos[idx] = vp;
         a.lags_pos[idx] = lp;
         a.vals_neg[idx] = vn;

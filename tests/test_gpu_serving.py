@@ -1,0 +1,101 @@
+"""GPU tests of the serving loop: query x resident-catalog results against
+the FP64 oracle, the top-K selection, continuous batching under a small HBM
+budget, and the same result alone and in the mix of concurrent requests."""
+import threading
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from seismic_gb300 import synth, xcorr
+
+pytestmark = pytest.mark.gpu
+
+
+def _catalog():
+    return synth.family_catalog(600, 3, 512, n_families=12, seed=71)
+
+
+def _fp64_block(cat, query, shift, b, e):
+    ev = np.concatenate([query, cat[b:e]])
+    nq = query.shape[0]
+    i = np.repeat(np.arange(nq), e - b)
+    j = nq + np.tile(np.arange(e - b), nq)
+    return O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(cat.shape[-1], shift))
+
+
+@pytest.mark.parametrize("form,tol", [("fp32", 1e-5), ("fp16", 1e-3)])
+def test_server_results_vs_fp64(cuda_ok, form, tol):
+    from seismic_gb300.serving import Server
+    cat = _catalog()
+    srv = Server(cat, shift=100, form=form, n_slots=3, max_query_events=16, topk=8)
+    query = synth.family_catalog(5, 3, 512, n_families=2, seed=72)
+    t = srv.submit(query, subset=(50, 480))
+    res = srv.wait(t)
+    r = _fp64_block(cat, query, 100, 50, 480)
+    ag = O.agreement(res.vals_pos.ravel(), res.lags_pos.ravel(), res.vals_neg.ravel(), res.lags_neg.ravel(), r,
+                     gap_tol=2 * tol)
+    assert ag.max_err_pos < tol and ag.max_err_neg < tol, ag
+    assert ag.lag_mismatch == 0, ag
+    # top-K: the K largest max-coefficients per query, ties to the lower index
+    for q in range(5):
+        order = np.lexsort((np.arange(430), -res.vals_pos[q]))[:8]
+        np.testing.assert_array_equal(res.topk_index[q], 50 + order)
+        np.testing.assert_array_equal(res.topk_vals[q], res.vals_pos[q][order])
+    assert res.latency_ms > 0
+    srv.close()
+
+
+def test_server_same_result_alone_and_in_the_mix(cuda_ok):
+    """A request gives bit-identical results alone and when it is admitted
+    while many other requests of different sizes are on the device."""
+    from seismic_gb300.serving import Server
+    cat = _catalog()
+    srv = Server(cat, shift=128, form="fp16", n_slots=4, max_query_events=32, topk=16)
+    probe = synth.family_catalog(7, 3, 512, n_families=2, seed=73)
+    alone = srv.wait(srv.submit(probe, subset=(10, 590)))
+    rng = np.random.default_rng(5)
+    tickets = []
+    lock = threading.Lock()
+
+    def burst(seed):
+        r = np.random.default_rng(seed)
+        for _ in range(6):
+            nq = int(r.integers(1, 33))
+            b = int(r.integers(0, 300))
+            e = int(r.integers(b + 1, 600))
+            t = srv.submit(synth.family_catalog(nq, 3, 512, n_families=1, seed=int(r.integers(1 << 30))), (b, e))
+            with lock:
+                tickets.append(t)
+
+    threads = [threading.Thread(target=burst, args=(s,)) for s in range(3)]
+    for th in threads:
+        th.start()
+    mid = srv.submit(probe, subset=(10, 590))
+    for th in threads:
+        th.join()
+    mixed = srv.wait(mid)
+    others = [srv.wait(t) for t in tickets]
+    assert len(others) == 18
+    for f in ("vals_pos", "lags_pos", "vals_neg", "lags_neg", "topk_vals", "topk_index"):
+        np.testing.assert_array_equal(getattr(alone, f), getattr(mixed, f))
+    assert srv.stats()["completed"] == 20
+    srv.close()
+    del rng
+
+
+def test_server_admission_by_hbm_budget(cuda_ok):
+    """With a pool that fits about one large request, requests still all
+    complete (admitted as memory frees up); one larger than the pool is
+    refused at submit."""
+    from seismic_gb300 import _lib
+    from seismic_gb300.serving import Server
+    cat = _catalog()
+    one = 2 * 8 * 600 * 16 + 3 * 8 * 3 * 512 * 4 * 3   # rough size of one 8-event full-catalog request, x2
+    srv = Server(cat, shift=64, form="fp32", n_slots=4, hbm_budget_bytes=one, max_query_events=64, topk=4)
+    ts = [srv.submit(synth.family_catalog(8, 3, 512, n_families=1, seed=80 + k)) for k in range(6)]
+    for t in ts:
+        srv.wait(t)
+    with pytest.raises(_lib.SeismicError):
+        srv.submit(synth.family_catalog(64, 3, 512, n_families=2, seed=90))
+    srv.close()
