@@ -148,9 +148,11 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
 
 /* Kernel (a) alone: packed half spectra and FP64 norms of every (event,
  * channel) row.  d_spectra: n_events*n_channels rows of padded_size/2
- * float2 (slot 0 = (Re X[0], Re X[P/2]), slot k = X[k]); d_norms:
- * n_events*n_channels doubles.  prescale != 0 scales each row by 1/norm
- * (0 for a zero row), the form the multichannel mean uses. */
+ * float2 (slot 0 = (Re X[0], Re X[P/2]), slot k = X[k]); d_norms: room for
+ * rows = n_events*n_channels doubles (the norms) followed by rows floats
+ * (1/norm computed in FP64 and rounded once, 0 for a zero row): 12*rows
+ * bytes.  prescale != 0 scales each row by 1/norm (0 for a zero row), the
+ * form the multichannel mean uses. */
 int seismic_spectra_device(const float *d_events, long long n_events, int n_channels, int event_length,
                            long long event_stride, long long channel_stride, int padded_size, int prescale,
                            void *d_spectra, double *d_norms, void *stream);
@@ -163,6 +165,20 @@ int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long
                          int form, float *d_vals_pos, int *d_lags_pos, float *d_vals_neg, int *d_lags_neg,
                          int *d_max_hist, int *d_min_hist, void *stream);
 
+/* seismic_pairs_device restricted to the work items [couple_begin,
+ * couple_end) of seismic_pair_couples(n_events, padded_size, n_channels):
+ * disjoint ranges on different GPUs (or streams) together cover the whole
+ * triangle with no exchange, each writing only its own pairs of the shared
+ * packed output layout.  Replaces the row partition of the reference's
+ * multi-GPU variant (Correlation_in_MultiCUDA/correlation_multicuda.cu:157-203). */
+int seismic_pairs_device_range(const void *d_spectra, const double *d_norms, long long n_events, int n_channels,
+                               int padded_size, int prescaled, int shift, float threshold, int n_classes_hist,
+                               long long couple_begin, long long couple_end, float *d_vals_pos, int *d_lags_pos,
+                               float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist, void *stream);
+/* Number of work items ("couples", two pairs each) of the triangle of
+ * n_events at this padded size and channel count. */
+long long seismic_pair_couples(long long n_events, int padded_size, int n_channels);
+
 /* seismic_xcorr_device for callers that cannot allocate device memory.
  * No counterpart in the reference: it exists for callers that must not call
  * cudaMalloc/cudaFree -- a host framework that has reserved nearly all of
@@ -173,7 +189,7 @@ int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long
  * the spectra and norms is one fixed array of seismic_noalloc_scratch_bytes()
  * (64 MiB) inside this library, reserved on every device that uses it until
  * the process exits.  Catalogs needing more than that
- * (n_events*n_channels*(padded_size*4 + 8) bytes, 256-byte rounded per part)
+ * (n_events*n_channels*(padded_size*4 + 12) bytes, 256-byte rounded per part)
  * are rejected with SEISMIC_ERR_WORKSPACE_TOO_SMALL.  The first call on a
  * device sets that device up, so make it before any stream capture.  All
  * calls share the scratch: calls that overlap on the GPU (other streams or

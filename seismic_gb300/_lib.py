@@ -60,6 +60,10 @@ def _declare(lib):
         "seismic_pairs_device": (ctypes.c_int, [vp, vp, c_ll, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_int, ctypes.c_float, ctypes.c_int, ctypes.c_int,
                                                 vp, vp, vp, vp, vp, vp, vp]),
+        "seismic_pairs_device_range": (ctypes.c_int, [vp, vp, c_ll, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                      ctypes.c_int, ctypes.c_float, ctypes.c_int, c_ll, c_ll,
+                                                      vp, vp, vp, vp, vp, vp, vp]),
+        "seismic_pair_couples": (c_ll, [c_ll, ctypes.c_int, ctypes.c_int]),
         "seismic_xcorr_device_noalloc": (ctypes.c_int, [vp, c_ll, ctypes.c_int, ctypes.c_int, c_ll, c_ll,
                                                         ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                         ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]),

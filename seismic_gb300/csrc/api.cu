@@ -118,7 +118,7 @@ static int form_stype(int form) {
 static size_t spectra_bytes(long long rows, int P, int stype = 0) {
   return align256((size_t)rows * (size_t)(P / 2) * (stype ? 4 : 8));
 }
-static size_t norms_bytes(long long rows) { return align256((size_t)rows * sizeof(double)); }
+static size_t norms_bytes(long long rows) { return norms_buffer_bytes(rows); }
 
 static int validate(long long n_events, int n_channels, int event_length, int padded, int shift,
                     int n_hist, int form) {
@@ -161,6 +161,7 @@ static int run_spectra(const DeviceState &st, const float *d_events, long long n
   sa.prescale = prescale;
   sa.spectra = spectra;
   sa.norms = norms;
+  sa.inv_norms = inverse_norms_of(norms, n * C);
   sa.twiddles = st.twiddles;
   SEISMIC_TRY(launch_spectra(P, sa, stream), "spectra kernel launch");
   g_launches.fetch_add(1);
@@ -169,11 +170,13 @@ static int run_spectra(const DeviceState &st, const float *d_events, long long n
 
 static int run_pairs(const DeviceState &st, const void *spectra, const double *norms, long long n, int C, int P,
                      int prescaled, int shift, float thr, int n_hist, float *vp, int *lp, float *vn, int *ln,
-                     int *hmax, int *hmin, cudaStream_t stream, int stype = 0) {
+                     int *hmax, int *hmin, cudaStream_t stream, int stype = 0, long long range_begin = 0,
+                     long long range_end = -1) {
   PairArgs pa{};  // zero: triangle mode, no query spectra
   pa.spectra = spectra;
   pa.stype = stype;
   pa.norms = norms;
+  pa.inv_norms = inverse_norms_of(norms, n * C);
   pa.n_events = n;
   pa.n_channels = C;
   pa.shift = shift;
@@ -190,15 +193,17 @@ static int run_pairs(const DeviceState &st, const void *spectra, const double *n
   const TuneEntry tune = tune_lookup(P, C);  // autotuner cache, else built-in defaults
   pa.tile = tune.tile;
   pa.twiddles = st.twiddles;
-  pa.couple_begin = 0;
-  pa.couple_end = pair_couples_total(n, pa.tile);
+  const long long total = pair_couples_total(n, pa.tile);
+  pa.couple_begin = range_begin < 0 ? 0 : (range_begin > total ? total : range_begin);
+  pa.couple_end = (range_end < 0 || range_end > total) ? total : range_end;
+  if (pa.couple_end <= pa.couple_begin) return SEISMIC_OK;
   static int ctas_cache[16] = {0};
   const int lp2 = 31 - __builtin_clz((unsigned)P);
   if (!ctas_cache[lp2]) ctas_cache[lp2] = pair_ctas_per_sm(P);
   const int ctas = (tune.ctas_per_sm > 0 && tune.ctas_per_sm < ctas_cache[lp2]) ? tune.ctas_per_sm : ctas_cache[lp2];
   const int G = P / 32;
   const int NG = (256 / G) > 0 ? (256 / G) : 1;
-  long long want = (pa.couple_end + NG - 1) / NG;
+  long long want = (pa.couple_end - pa.couple_begin + NG - 1) / NG;
   long long grid = (long long)st.sm_count * ctas;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
@@ -379,6 +384,34 @@ int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long
   return run_pairs(*st, reinterpret_cast<const float2 *>(d_spectra), d_norms, n_events, n_channels, padded_size,
                    prescaled ? 1 : 0, shift, threshold, n_classes_hist, d_vals_pos, d_lags_pos, d_vals_neg,
                    d_lags_neg, d_max_hist, d_min_hist, (cudaStream_t)stream);
+}
+
+long long seismic_pair_couples(long long n_events, int padded_size, int n_channels) {
+  if (n_events < 1 || n_channels < 1 || !supported_padded_size(padded_size)) return 0;
+  return pair_couples_total(n_events, tune_lookup(padded_size, n_channels).tile);
+}
+
+int seismic_pairs_device_range(const void *d_spectra, const double *d_norms, long long n_events, int n_channels,
+                               int padded_size, int prescaled, int shift, float threshold, int n_classes_hist,
+                               long long couple_begin, long long couple_end, float *d_vals_pos, int *d_lags_pos,
+                               float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist, void *stream) {
+  set_status(SEISMIC_OK, "");
+  int s = validate(n_events, n_channels, 1, padded_size, shift, n_classes_hist, SEISMIC_FORM_FP32);
+  if (s) return s;
+  if (!d_spectra || !d_norms || !d_vals_pos || !d_lags_pos || !d_vals_neg || !d_lags_neg)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");
+  if (n_classes_hist > 0 && (!d_max_hist || !d_min_hist))
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null histogram buffer");
+  if (n_channels > 1 && !prescaled)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "multichannel spectra must be prescaled");
+  if (couple_begin < 0 || couple_end < couple_begin)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "bad couple range");
+  int dev;
+  DeviceState *st;
+  if ((s = ensure_device(&dev, &st))) return s;
+  return run_pairs(*st, d_spectra, d_norms, n_events, n_channels, padded_size, prescaled ? 1 : 0, shift, threshold,
+                   n_classes_hist, d_vals_pos, d_lags_pos, d_vals_neg, d_lags_neg, d_max_hist, d_min_hist,
+                   (cudaStream_t)stream, 0, couple_begin, couple_end);
 }
 
 int seismic_xcorr_host(const float *events, long long n_events, int n_channels, int event_length,

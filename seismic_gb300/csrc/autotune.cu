@@ -160,7 +160,7 @@ extern "C" int seismic_autotune(int padded_size, int n_channels, const char *cac
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t e = cudaMalloc(&ev, sizeof(float) * rows * L);
   if (e == cudaSuccess) e = cudaMalloc(&spec, sizeof(float2) * rows * (P / 2));
-  if (e == cudaSuccess) e = cudaMalloc(&norms, sizeof(double) * rows);
+  if (e == cudaSuccess) e = cudaMalloc(&norms, norms_buffer_bytes(rows));
   if (e == cudaSuccess) e = cudaMalloc(&vp, sizeof(float) * npairs);
   if (e == cudaSuccess) e = cudaMalloc(&vn, sizeof(float) * npairs);
   if (e == cudaSuccess) e = cudaMalloc(&lp, sizeof(int) * npairs);
@@ -197,6 +197,7 @@ extern "C" int seismic_autotune(int padded_size, int n_channels, const char *cac
   sa.stype = 0;
   sa.spectra = spec;
   sa.norms = norms;
+  sa.inv_norms = inverse_norms_of(norms, rows);
   sa.twiddles = tw;
   e = launch_spectra(P, sa, st);
   note_launches(2);
@@ -206,6 +207,7 @@ extern "C" int seismic_autotune(int padded_size, int n_channels, const char *cac
   pa.spectra = spec;
   pa.stype = 0;
   pa.norms = norms;
+  pa.inv_norms = inverse_norms_of(norms, rows);
   pa.n_events = n;
   pa.n_channels = C;
   pa.shift = P / 2;

@@ -126,7 +126,7 @@ extern "C" int seismic_batch_create(const seismic_catalog *catalogs, int n_catal
     const long long rows = c.n_events * c.n_channels;
     ws_off[k] = ws_total;
     spec_bytes[k] = ((size_t)rows * (P / 2) * sizeof(float2) + 255) / 256 * 256;
-    ws_total += spec_bytes[k] + ((size_t)rows * sizeof(double) + 255) / 256 * 256;
+    ws_total += spec_bytes[k] + norms_buffer_bytes(rows);
     max_hist = std::max(max_hist, c.n_classes_hist);
     total_pairs += c.n_events * (c.n_events + 1) / 2;
     cats[k].P = P;
@@ -166,12 +166,14 @@ extern "C" int seismic_batch_create(const seismic_catalog *catalogs, int n_catal
     sa.stype = 0;
     sa.spectra = ws;
     sa.norms = norms;
+    sa.inv_norms = inverse_norms_of(norms, rows);
     sa.twiddles = tw;
     PairArgs &pa = cats[k].pairs;
     std::memset(&pa, 0, sizeof(pa));
     pa.spectra = ws;
     pa.stype = 0;
     pa.norms = norms;
+    pa.inv_norms = inverse_norms_of(norms, rows);
     pa.n_events = c.n_events;
     pa.n_channels = C;
     pa.shift = c.shift;

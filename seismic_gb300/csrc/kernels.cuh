@@ -26,13 +26,25 @@ struct SpectraArgs {
   int stype;               // spectrum storage: 0 float2, 1 half2 (FP16), 2 bfloat162 (BF16)
   void *spectra;           // out [n_events*n_channels][P/2] of stype
   double *norms;           // out [n_events*n_channels], FP64 L2 norms
+  float *inv_norms;        // out [n_events*n_channels], 1/norm computed in FP64, rounded once (0 for 0)
   const float2 *twiddles;  // twiddle_table()
 };
+
+// A norms buffer holds `rows` FP64 norms followed by `rows` FP32 inverse norms.
+inline size_t norms_buffer_bytes(long long rows) { return ((size_t)rows * 12 + 255) / 256 * 256; }
+__host__ __device__ inline float *inverse_norms_of(double *norms, long long rows) {
+  return reinterpret_cast<float *>(norms + rows);
+}
+__host__ __device__ inline const float *inverse_norms_of(const double *norms, long long rows) {
+  return reinterpret_cast<const float *>(norms + rows);
+}
 
 struct PairArgs {
   const void *spectra;     // [n_events*n_channels][P/2] of stype
   int stype;               // 0 float2, 1 half2, 2 bfloat162
   const double *norms;     // [n_events*n_channels]
+  const float *inv_norms;  // [n_events*n_channels], see SpectraArgs
+  const float *inv_norms_q;  // rectangle mode: the queries' inverse norms
   long long n_events;
   int n_channels;
   int shift;               // lags d = 1-shift .. shift

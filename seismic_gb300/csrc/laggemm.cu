@@ -80,7 +80,10 @@ __global__ void lag_prep_kernel(const float *__restrict__ ev, long long n, int C
     dh[k] = h;
     dl[k] = __float2bfloat16_rn(v - __bfloat162float(h));
   }
-  if (lane == 0) norms[row] = nrm;
+  if (lane == 0) {
+    norms[row] = nrm;
+    inverse_norms_of(norms, n * C)[row] = nrm > 0.0 ? (float)(1.0 / nrm) : 0.f;
+  }
 }
 
 // ------------------------------------------------------------------ main
@@ -395,21 +398,23 @@ __global__ void __launch_bounds__(kLagThreads, 1)
             }
           }
           if (i < N && j >= i) {
-            double denom;
+            // per-event 1/norm factors come from FP64 (prep kernel); per pair FP32
+            const float *inv = inverse_norms_of(a.norms, N * C);
+            float scale;
             bool live = false;
             if (a.prescaled) {
-              for (int cc = 0; cc < C; ++cc) live |= (a.norms[i * C + cc] > 0.0) && (a.norms[j * C + cc] > 0.0);
-              denom = (double)C;
+              for (int cc = 0; cc < C; ++cc) live |= (inv[i * C + cc] > 0.f) && (inv[j * C + cc] > 0.f);
+              scale = 1.0f / (float)C;
             } else {
-              const double ni = a.norms[i * C], nj = a.norms[j * C];
-              live = ni > 0.0 && nj > 0.0;
-              denom = ni * nj;
+              const float ni = inv[i * C], nj = inv[j * C];
+              live = ni > 0.f && nj > 0.f;
+              scale = ni * nj;
             }
             float vp = 0.f, vn = 0.f;
             int lp = 0, ln = 0;
             if (live) {
-              vp = (float)((double)best / denom);
-              vn = (float)((double)worst / denom);
+              vp = best * scale;
+              vn = worst * scale;
               lp = best > 0.f ? a.shift - bn : 0;
               ln = worst < 0.f ? a.shift - wn : 0;
               if (a.n_hist > 0) {
@@ -527,7 +532,7 @@ LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int 
 size_t lag_workspace_bytes(long long n, int C, int length) {
   const int lp = (length + kLagKC - 1) / kLagKC * kLagKC;
   const size_t x = (size_t)n * C * lp * 2;
-  return 2 * ((x + 255) / 256 * 256) + ((size_t)n * C * 8 + 255) / 256 * 256 + 256;
+  return 2 * ((x + 255) / 256 * 256) + norms_buffer_bytes(n * C) + 256;
 }
 
 cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length, long long ev_stride,

@@ -103,11 +103,11 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
 
   const long long rows = n_events * n_channels;
   const size_t spec_b = round256((size_t)rows * (size_t)(padded_size / 2) * sizeof(float2));
-  const size_t norm_b = round256((size_t)rows * sizeof(double));
+  const size_t norm_b = norms_buffer_bytes(rows);  // FP64 norms + FP32 inverse norms
   if (spec_b + norm_b > kNoAllocScratchBytes) {
     char msg[200];
     snprintf(msg, sizeof(msg),
-             "catalog needs %zu bytes of scratch (n_events*n_channels*(padded_size*4 + 8)); "
+             "catalog needs %zu bytes of scratch (n_events*n_channels*(padded_size*4 + 12)); "
              "the no-alloc entry point has %zu",
              spec_b + norm_b, kNoAllocScratchBytes);
     return report_status(SEISMIC_ERR_WORKSPACE_TOO_SMALL, msg);
@@ -131,6 +131,7 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   sa.stype = 0;  // FP32 spectra
   sa.spectra = spectra;
   sa.norms = norms;
+  sa.inv_norms = inverse_norms_of(norms, rows);
   sa.twiddles = d->twiddles;
   cudaError_t e = launch_spectra(padded_size, sa, st);
   if (e != cudaSuccess) return report_cuda(e, "spectra kernel launch");
@@ -139,6 +140,7 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   PairArgs pa{};
   pa.spectra = spectra;
   pa.norms = norms;
+  pa.inv_norms = inverse_norms_of(norms, rows);
   pa.n_events = n_events;
   pa.n_channels = n_channels;
   pa.shift = shift;

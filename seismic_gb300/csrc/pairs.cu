@@ -375,29 +375,32 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
       }
     }
 
-    // ---- epilogue: normalise (FP64), histogram, threshold, packed write
+    // ---- epilogue: normalise, histogram, threshold, packed write.  The
+    //      per-event factors 1/norm were computed in FP64 by the spectra
+    //      kernel and rounded once; the per-pair scaling is FP32 (<= 4 ulp),
+    //      which keeps the slow FP64 pipe out of the pair loop.
     if (t == 0) {
+      const float *inv_i = a.rect ? a.inv_norms_q : a.inv_norms;
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
         if (p == 1 && !out_b) break;
         const long long j = p == 0 ? ja : jb;
         const unsigned kp = key[2 * p], kn = key[2 * p + 1];
-        const double *norms_i = a.rect ? a.norms_q : a.norms;
-        double denom;
+        float scale;
         bool live = false;
-        if (a.prescaled) {
-          for (int c = 0; c < C; ++c) live |= (norms_i[i * C + c] > 0.0) && (a.norms[j * C + c] > 0.0);
-          denom = (double)P * (double)C;
+        if (a.prescaled) {  // spectra already carry 1/norm: mean over channels
+          for (int c = 0; c < C; ++c) live |= (inv_i[i * C + c] > 0.f) && (a.inv_norms[j * C + c] > 0.f);
+          scale = 1.0f / ((float)P * (float)C);
         } else {
-          const double ni = norms_i[i * C], nj = a.norms[j * C];
-          live = ni > 0.0 && nj > 0.0;
-          denom = (double)P * ni * nj;
+          const float ni = inv_i[i * C], nj = a.inv_norms[j * C];
+          live = ni > 0.f && nj > 0.f;
+          scale = (ni * nj) * (1.0f / (float)P);
         }
         float vp = 0.f, vn = 0.f;
         int lp = 0, ln = 0;
         if (live) {
-          vp = (float)((double)__uint_as_float(kp) / denom);
-          vn = -(float)((double)__uint_as_float(kn) / denom);
+          vp = __uint_as_float(kp) * scale;
+          vn = -(__uint_as_float(kn) * scale);
           lp = kp ? lag[2 * p] : 0;
           ln = kn ? lag[2 * p + 1] : 0;
           if (a.n_hist > 0) {

@@ -172,7 +172,7 @@ size_t request_bytes(const seismic_server *s, int nq, long long ncols) {
   const size_t rows = (size_t)nq * s->C;
   size_t b = round256(rows * s->L * sizeof(float));                             // query events
   b += round256(rows * (s->P / 2) * (s->stype ? 4 : 8));                        // query spectra
-  b += round256(rows * sizeof(double));                                         // query norms
+  b += norms_buffer_bytes((long long)rows);                                     // query norms
   b += 4 * round256((size_t)nq * ncols * 4);                                    // outputs
   b += round256((size_t)nq * s->topk * 4) + round256((size_t)nq * s->topk * 8);  // top-K
   return b;
@@ -235,7 +235,7 @@ int launch_request(seismic_server *s, Request *r) {
   void *q_spec = base;
   base += round256(rows * (s->P / 2) * (s->stype ? 4 : 8));
   double *q_norm = reinterpret_cast<double *>(base);
-  base += round256(rows * sizeof(double));
+  base += norms_buffer_bytes((long long)rows);
   const size_t ob = round256((size_t)nq * r->n_cols * 4);
   float *d_vp = reinterpret_cast<float *>(base);
   int *d_lp = reinterpret_cast<int *>(base + ob);
@@ -257,14 +257,17 @@ int launch_request(seismic_server *s, Request *r) {
   sa.stype = s->stype;
   sa.spectra = q_spec;
   sa.norms = q_norm;
+  sa.inv_norms = inverse_norms_of(q_norm, (long long)rows);
   sa.twiddles = s->tw;
   if (e == cudaSuccess) e = launch_spectra(s->P, sa, st);
   PairArgs pa{};
   pa.rect = 1;
   pa.spectra = s->cat_spectra;
   pa.norms = s->cat_norms;
+  pa.inv_norms = inverse_norms_of(s->cat_norms, s->n_cat * s->C);
   pa.spectra_q = q_spec;
   pa.norms_q = q_norm;
+  pa.inv_norms_q = inverse_norms_of(q_norm, (long long)rows);
   pa.stype = s->stype;
   pa.n_query = nq;
   pa.col_begin = r->col_begin;
@@ -390,7 +393,7 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   const long long rows = n_catalog * n_channels;
   float *d_cat = nullptr;
   cudaError_t e = cudaMalloc(&s->cat_spectra, (size_t)rows * (P / 2) * (s->stype ? 4 : 8));
-  if (e == cudaSuccess) e = cudaMalloc(&s->cat_norms, (size_t)rows * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&s->cat_norms, norms_buffer_bytes(rows));
   if (e == cudaSuccess) e = cudaMalloc(&d_cat, (size_t)rows * event_length * sizeof(float));
   if (e == cudaSuccess)
     e = cudaMemcpy(d_cat, catalog, (size_t)rows * event_length * sizeof(float), cudaMemcpyHostToDevice);
@@ -406,6 +409,7 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
     sa.stype = s->stype;
     sa.spectra = s->cat_spectra;
     sa.norms = s->cat_norms;
+    sa.inv_norms = inverse_norms_of(s->cat_norms, rows);
     sa.twiddles = tw;
     e = launch_spectra(P, sa, nullptr);
     note_launches(1);

@@ -184,7 +184,11 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
   }
   if (t == 0) {
     a.norms[row_a] = na;
-    if (has_b) a.norms[row_b] = nb;
+    a.inv_norms[row_a] = na > 0.0 ? (float)(1.0 / na) : 0.f;
+    if (has_b) {
+      a.norms[row_b] = nb;
+      a.inv_norms[row_b] = nb > 0.0 ? (float)(1.0 / nb) : 0.f;
+    }
   }
 }
 

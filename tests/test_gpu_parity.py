@@ -143,6 +143,42 @@ def test_device_api_torch_stream_and_workspace(cuda_ok):
         xcorr.xcorr(t, 200, workspace=small)
 
 
+def test_pair_ranges_on_streams_compose_the_triangle(cuda_ok):
+    """Disjoint work-item ranges (how ranks or streams share one catalog)
+    write exactly what one full launch writes."""
+    import ctypes
+    import torch
+    from seismic_gb300 import _lib
+    from seismic_gb300.shard import couple_range
+    lib = _lib.lib()
+    ev = synth.family_catalog(150, 3, 700, n_families=5, seed=91)
+    n, c, length = ev.shape
+    p = xcorr.resolve_padded_size(length, 300)
+    t = torch.from_numpy(ev).cuda()
+    rows = n * c
+    spec = torch.empty(rows * p // 2 * 2, device="cuda")
+    norms = torch.empty(rows + (rows + 1) // 2, dtype=torch.float64, device="cuda")
+    _lib.check(lib.seismic_spectra_device(t.data_ptr(), n, c, length, c * length, length, p, 1, spec.data_ptr(),
+                                          norms.data_ptr(), None))
+    m = n * (n + 1) // 2
+    full = [torch.zeros(m, device="cuda"), torch.zeros(m, dtype=torch.int32, device="cuda"),
+            torch.zeros(m, device="cuda"), torch.zeros(m, dtype=torch.int32, device="cuda")]
+    parts = [torch.full((m,), float("nan"), device="cuda"), torch.zeros(m, dtype=torch.int32, device="cuda"),
+             torch.full((m,), float("nan"), device="cuda"), torch.zeros(m, dtype=torch.int32, device="cuda")]
+    _lib.check(lib.seismic_pairs_device(spec.data_ptr(), norms.data_ptr(), n, c, p, 1, 300, 0.0, 0, 0,
+                                        *(x.data_ptr() for x in full), None, None, None))
+    total = lib.seismic_pair_couples(n, p, c)
+    streams = [torch.cuda.Stream() for _ in range(3)]
+    for r, s in enumerate(streams):
+        b, e = couple_range(total, 3, r)
+        _lib.check(lib.seismic_pairs_device_range(spec.data_ptr(), norms.data_ptr(), n, c, p, 1, 300, 0.0, 0, b, e,
+                                                  *(x.data_ptr() for x in parts), None, None,
+                                                  ctypes.c_void_p(s.cuda_stream)))
+    torch.cuda.synchronize()
+    for a, b in zip(full, parts):
+        assert torch.equal(a, b)
+
+
 def test_precision_workload_size_properties(cuda_ok):
     """Full-size N=16384, L=1024, +-128 lags: properties that hold at any size
     (diagonal coefficient 1 at lag 0, |coef| <= 1, histogram totals) and an

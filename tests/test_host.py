@@ -73,10 +73,15 @@ def _scheduler_pairs(n, tile):
     """Python restatement of the pair kernel's work decomposition
     (decode_tile + couple split in pairs.cu) to check coverage."""
     nb = (n + tile - 1) // tile
+    return _scheduler_pairs_range(n, tile, 0, nb * (nb + 1) // 2 * (tile * tile // 2))
+
+
+def _scheduler_pairs_range(n, tile, begin, end):
+    """Pairs produced by work items [begin, end) of the triangle of n events."""
+    nb = (n + tile - 1) // tile
     cpt = tile * tile // 2
-    total = nb * (nb + 1) // 2 * cpt
     seen = []
-    for w in range(total):
+    for w in range(begin, end):
         tl, lc = divmod(w, cpt)
         twonb1 = 2.0 * nb + 1.0
         b = int((twonb1 - np.sqrt(twonb1 * twonb1 - 8.0 * tl)) * 0.5)
