@@ -193,23 +193,34 @@ static int run_pairs(const DeviceState &st, const void *spectra, const double *n
   const TuneEntry tune = tune_lookup(P, C);  // autotuner cache, else built-in defaults
   pa.tile = tune.tile;
   pa.twiddles = st.twiddles;
-  const long long total = pair_couples_total(n, pa.tile);
+  pa.error_flag = st.error_flag;
+  const long long total = pair_work_total(P, pa);
   pa.couple_begin = range_begin < 0 ? 0 : (range_begin > total ? total : range_begin);
   pa.couple_end = (range_end < 0 || range_end > total) ? total : range_end;
   if (pa.couple_end <= pa.couple_begin) return SEISMIC_OK;
+  SEISMIC_TRY(launch_pair_work(P, pa, st.sm_count, tune.ctas_per_sm, stream), "pair kernel launch");
+  g_launches.fetch_add(1);
+  return SEISMIC_OK;
+}
+
+long long pair_work_total(int P, const PairArgs &a) {
+  if (staged_supported(P, a)) return staged_items_total(P, a);
+  return a.rect ? rect_couples_total(a.n_query, a.n_cols, a.tile) : pair_couples_total(a.n_events, a.tile);
+}
+
+cudaError_t launch_pair_work(int P, const PairArgs &a, int sm_count, int ctas_per_sm, cudaStream_t stream) {
+  if (a.couple_end <= a.couple_begin) return cudaSuccess;
+  if (staged_supported(P, a)) return launch_pairs_staged(P, a, sm_count, stream);
   static int ctas_cache[16] = {0};
   const int lp2 = 31 - __builtin_clz((unsigned)P);
   if (!ctas_cache[lp2]) ctas_cache[lp2] = pair_ctas_per_sm(P);
-  const int ctas = (tune.ctas_per_sm > 0 && tune.ctas_per_sm < ctas_cache[lp2]) ? tune.ctas_per_sm : ctas_cache[lp2];
-  const int G = P / 32;
-  const int NG = (256 / G) > 0 ? (256 / G) : 1;
-  long long want = (pa.couple_end - pa.couple_begin + NG - 1) / NG;
-  long long grid = (long long)st.sm_count * ctas;
+  const int ctas = (ctas_per_sm > 0 && ctas_per_sm < ctas_cache[lp2]) ? ctas_per_sm : ctas_cache[lp2];
+  const int NG = groups_per_cta(P);
+  long long want = (a.couple_end - a.couple_begin + NG - 1) / NG;
+  long long grid = (long long)sm_count * ctas;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
-  SEISMIC_TRY(launch_pairs(P, pa, (int)grid, stream), "pair kernel launch");
-  g_launches.fetch_add(1);
-  return SEISMIC_OK;
+  return launch_pairs(P, a, (int)grid, stream);
 }
 
 int device_context(int *sm_count, const float2 **twiddles, int **error_flag) {
@@ -376,6 +387,8 @@ int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null histogram buffer");
   if (form != SEISMIC_FORM_FP32)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "seismic_pairs_device pairs FP32 spectra (form 0)");
+  if (reinterpret_cast<uintptr_t>(d_spectra) & 15u)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "spectra must be 16-byte aligned");
   if (n_channels > 1 && !prescaled)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "multichannel spectra must be prescaled");
   int dev;
@@ -388,7 +401,11 @@ int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long
 
 long long seismic_pair_couples(long long n_events, int padded_size, int n_channels) {
   if (n_events < 1 || n_channels < 1 || !supported_padded_size(padded_size)) return 0;
-  return pair_couples_total(n_events, tune_lookup(padded_size, n_channels).tile);
+  PairArgs pa{};  // FP32 spectra at an aligned address, triangle mode
+  pa.n_events = n_events;
+  pa.n_channels = n_channels;
+  pa.tile = tune_lookup(padded_size, n_channels).tile;
+  return pair_work_total(padded_size, pa);
 }
 
 int seismic_pairs_device_range(const void *d_spectra, const double *d_norms, long long n_events, int n_channels,
@@ -406,6 +423,8 @@ int seismic_pairs_device_range(const void *d_spectra, const double *d_norms, lon
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "multichannel spectra must be prescaled");
   if (couple_begin < 0 || couple_end < couple_begin)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "bad couple range");
+  if (reinterpret_cast<uintptr_t>(d_spectra) & 15u)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "spectra must be 16-byte aligned");
   int dev;
   DeviceState *st;
   if ((s = ensure_device(&dev, &st))) return s;

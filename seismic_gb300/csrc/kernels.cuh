@@ -75,7 +75,27 @@ struct PairArgs {
   long long n_query;
   long long col_begin;
   long long n_cols;
+  // Staged form (pairs_staged.cu) only: tile columns per L2 band of the
+  // triangle walk, the shared-memory ring depth, and the device error flag
+  // set when a bounded wait runs out.
+  int band_tiles;
+  int ring;
+  int *error_flag;
 };
+
+// ---- staged pair form (pairs_staged.cu): spectra staged into shared memory
+// by TMA (P = 4096 by default).  Work items are (event i, T consecutive j).
+bool staged_supported(int P, const PairArgs &a);
+long long staged_items_total(int P, const PairArgs &a);  // triangle or rectangle
+// Launches items [a.couple_begin, a.couple_end) of the staged decomposition.
+cudaError_t launch_pairs_staged(int P, const PairArgs &a, int sm_count, cudaStream_t s);
+
+// Pair-form dispatch (api.cu): the staged form where staged_supported, else
+// the direct form with a.tile.  pair_work_total is the item count of the
+// form launch_pair_work runs for `a`; ctas_per_sm (0 = occupancy maximum)
+// applies to the direct form.
+long long pair_work_total(int P, const PairArgs &a);
+cudaError_t launch_pair_work(int P, const PairArgs &a, int sm_count, int ctas_per_sm, cudaStream_t s);
 // Couples covering a rectangle of n_query x n_cols pairs with chunk width `tile`.
 long long rect_couples_total(long long n_query, long long n_cols, int tile);
 

@@ -41,6 +41,7 @@
 
 #include "kernels.cuh"
 #include "tcgen05.cuh"
+#include "tma_host.cuh"
 
 namespace seismic {
 
@@ -469,25 +470,8 @@ int *device_error_flag() {
   return static_cast<int *>(p);
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
-  return fn;
-}
-
 static bool make_map(CUtensorMap *m, const void *ptr, long long rows, int lp) {
-  EncodeTiledFn fn = encode_fn();
+  EncodeTiledFn fn = tensor_map_encoder();
   if (!fn) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)lp, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)lp * 2};

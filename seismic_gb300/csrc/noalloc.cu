@@ -44,6 +44,7 @@ struct NoAllocDevice {
   bool ready = false;
   unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
   const float2 *twiddles = nullptr;
+  int *error_flag = nullptr;  // device flag set by a bounded wait that ran out
   int sm_count = 0;
 };
 
@@ -72,6 +73,8 @@ int noalloc_setup(NoAllocDevice **out) {
     note_launches(1);
     d.twiddles = twiddle_table();
     if (!d.twiddles) return report_status(SEISMIC_ERR_CUDA, "twiddle table address");
+    d.error_flag = device_error_flag();
+    if (!d.error_flag) return report_status(SEISMIC_ERR_CUDA, "device error flag address");
     d.scratch = static_cast<unsigned char *>(p);
     d.ready = true;
   }
@@ -157,15 +160,10 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   pa.min_hist = d_min_hist;
   pa.tile = pair_tile_for(padded_size);
   pa.twiddles = d->twiddles;
+  pa.error_flag = d->error_flag;
   pa.couple_begin = 0;
-  pa.couple_end = pair_couples_total(n_events, pa.tile);
-  const int G = padded_size / 32;
-  const int NG = (256 / G) > 0 ? (256 / G) : 1;
-  long long want = (pa.couple_end + NG - 1) / NG;
-  long long grid = (long long)d->sm_count * pair_ctas_per_sm(padded_size);
-  if (want < grid) grid = want;
-  if (grid < 1) grid = 1;
-  e = launch_pairs(padded_size, pa, (int)grid, st);
+  pa.couple_end = pair_work_total(padded_size, pa);
+  e = launch_pair_work(padded_size, pa, d->sm_count, 0, st);
   if (e != cudaSuccess) return report_cuda(e, "pair kernel launch");
   note_launches(1);
   return SEISMIC_OK;

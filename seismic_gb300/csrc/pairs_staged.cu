@@ -1,0 +1,365 @@
+// Kernels (b) + (c), staged form: the pair-tile kernel with its spectra
+// staged into shared memory by TMA.  Same results as the direct form
+// (pairs.cu); replaces the same reference code:
+//   ElementWiseMultiplication  Correlation_in_OMP/correlation_c.cpp:188-193
+//   inverseFFT                 Correlation_in_OMP/correlation_c.cpp:58-137
+//   the dynamic row loop       Correlation_in_OMP/correlation_c.cpp:251-293
+//
+// Work item = one event i and a block of T = 2 NG consecutive events
+// j0 .. j0+T-1; group g of the CTA's NG FFT groups takes the couple
+// (i; j0+2g, j0+2g+1) -- the same couples as the direct form, so both forms
+// give bit-identical results.  The items of the upper triangle are square
+// tiles of T x T events (T items per tile, one per i), walked in column
+// bands of `band_tiles` tiles so the j spectra of a band stay in L2 while
+// every row above the band passes over it; the rectangle (query x catalog)
+// walks column blocks, all queries per block.
+//
+// Pipeline.  Each item's spectra are cut into units (channel c, chunk r):
+// bins [r S, (r+1) S) of row i and of the T rows j0..j0+T-1, exactly the
+// bins ca + r S and cb + r S every FFT thread reads at step r
+// (pair_core.cuh).  A producer warp (one elected thread) streams units into
+// a ring of K shared-memory slots: a 1-D bulk copy for row i's chunk and one
+// 3-D TMA box {S bins, 1 channel, T events} for the j rows (rows past the
+// catalog are zero-filled by the TMA unit), completing on the slot's `full`
+// mbarrier; the FFT warps conj-multiply from the slot and release it on its
+// `empty` mbarrier.  While the groups run their inverse FFTs the producer
+// fills the ring with the next item's first units, so spectra reads leave
+// the critical path.  Row i is staged once per unit for all NG groups:
+// 1 + T rows per T pairs instead of 3 rows per 2.
+//
+// Every mbarrier wait is bounded; one that runs out sets the device error
+// flag and the CTA finishes its items without waiting further (results are
+// then invalid, and the host reports SEISMIC_ERR_DEVICE_TIMEOUT).
+#include <cstdlib>
+#include <cstring>
+
+#include "pair_core.cuh"
+#include "tcgen05.cuh"
+#include "tma_host.cuh"
+
+namespace seismic {
+
+constexpr int kStagedHistMax = 1024;  // larger histograms use global atomics
+constexpr int kStagedRingMax = 16;
+constexpr size_t kStagedSmemBudget = 227 * 1024;
+
+template <int P, int NWARP> struct Staged {
+  static constexpr int G = P / 32;
+  static constexpr int NG = NWARP * 32 / G;  // FFT groups per CTA
+  static constexpr int T = 2 * NG;           // j events per item = tile side; T items per tile
+  static constexpr int ROWS = 1 + T;         // staged rows per unit: i, j0 .. j0+T-1
+  static constexpr int S = P / 16;
+  static constexpr int NW = (G + 31) / 32;
+  static constexpr int CONSUMERS = NWARP * 32;  // FFT threads
+  static constexpr int THREADS = CONSUMERS + 32;  // + the producer warp
+  static constexpr size_t EX_BYTES = (size_t)NG * padded_len<P>() * sizeof(float2);
+  static constexpr size_t RED_BYTES = (size_t)NG * NW * 8 * sizeof(unsigned);
+  static constexpr size_t PROD_OFF = (EX_BYTES + RED_BYTES + 15) / 16 * 16;
+  static constexpr size_t RING_OFF = (PROD_OFF + 64 + 127) / 128 * 128;
+  template <int ST> static constexpr size_t unit_bytes() {
+    return (size_t)ROWS * S * sizeof(typename SpecT<ST>::T);
+  }
+};
+
+// Item w -> (i, j0).  Triangle: tile x = w / T in band order, i = bi T + w % T.
+__host__ __device__ __forceinline__ void staged_decode(const PairArgs &a, int T, long long w, long long &i,
+                                                       long long &j0) {
+  if (a.rect) {
+    const long long blk = w / a.n_query;
+    i = w - blk * a.n_query;
+    j0 = a.col_begin + blk * T;
+    return;
+  }
+  const long long nb = (a.n_events + T - 1) / T;
+  long long x = w / T;
+  const long long ii = w - x * T;
+  const long long band = a.band_tiles > 0 ? a.band_tiles : nb;
+  long long b0 = 0;  // first tile column of the band
+  for (;;) {
+    const long long be = b0 + band < nb ? b0 + band : nb;
+    const long long wb = be - b0;
+    const long long cnt = b0 * wb + wb * (wb + 1) / 2;
+    if (x < cnt || be >= nb) {
+      long long bi, bj;
+      if (x < b0 * wb) {  // rows above the band: full width
+        bi = x / wb;
+        bj = b0 + (x - bi * wb);
+      } else {            // the band's own triangle
+        long long r, c;
+#ifdef __CUDA_ARCH__
+        decode_tile(x - b0 * wb, wb, r, c);
+#else
+        const long long xx = x - b0 * wb;
+        r = 0;
+        while (tri_start(r + 1, wb) <= xx) ++r;
+        c = r + (xx - tri_start(r, wb));
+#endif
+        bi = b0 + r;
+        bj = b0 + c;
+      }
+      i = bi * T + ii;
+      j0 = bj * T;
+      return;
+    }
+    x -= cnt;
+    b0 = be;
+  }
+}
+
+__device__ __forceinline__ void staged_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err) {
+  if (*abort_flag) {
+    (void)tc::mbar_try_wait(bar, parity);
+    return;
+  }
+  if (!tc::mbar_wait(bar, parity)) {
+    *abort_flag = 1;
+    if (err) atomicExch(err, 1);
+  }
+}
+
+// Cursor of the next unit to stage (shared memory, used by the producer only).
+struct StagedCursor {
+  long long w, i, j0;
+  int c, r;
+};
+
+template <int P, int NWARP, int ST>
+__device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMap *jmap, StagedCursor *cur,
+                                             unsigned char *dst, uint64_t *full) {
+  using SH = Staged<P, NWARP>;
+  using ST_T = typename SpecT<ST>::T;
+  constexpr int S = SH::S, H = P / 2;
+  constexpr uint32_t CHUNK = (uint32_t)(S * sizeof(ST_T));
+  const int C = a.n_channels;
+  const ST_T *spec_i = reinterpret_cast<const ST_T *>(a.rect ? a.spectra_q : a.spectra);
+  const long long n_i = a.rect ? a.n_query : a.n_events;
+  const long long i = cur->i < n_i ? cur->i : n_i - 1;  // ragged last tile row: staged but unused
+  const int c = cur->c, r = cur->r;
+  tc::mbar_arrive_expect_tx(full, (uint32_t)SH::template unit_bytes<ST>());
+  tc::bulk_load(dst, spec_i + (i * C + c) * (long long)H + r * S, CHUNK, full);
+  tc::tma_load_3d(dst + CHUNK, jmap, r * S, c, (int)cur->j0, full);
+  if (++cur->r == 8) {
+    cur->r = 0;
+    if (++cur->c == C) {
+      cur->c = 0;
+      cur->w += gridDim.x;
+      if (cur->w < a.couple_end) staged_decode(a, SH::T, cur->w, cur->i, cur->j0);
+    }
+  }
+}
+
+template <int P, int NWARP, int ST>
+__global__ void __launch_bounds__(NWARP * 32 + 32, 1)
+    staged_pair_kernel(const PairArgs a, const __grid_constant__ CUtensorMap jmap) {
+  using SH = Staged<P, NWARP>;
+  using ST_T = typename SpecT<ST>::T;
+  constexpr int G = SH::G, T = SH::T, S = SH::S, NW = SH::NW;
+  constexpr uint32_t UNIT = (uint32_t)SH::template unit_bytes<ST>();
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  float2 *bufs = reinterpret_cast<float2 *>(smem);
+  unsigned *reds = reinterpret_cast<unsigned *>(smem + SH::EX_BYTES);
+  StagedCursor *cur = reinterpret_cast<StagedCursor *>(smem + SH::PROD_OFF);
+  volatile int *s_abort = reinterpret_cast<volatile int *>(smem + SH::PROD_OFF + 48);
+  unsigned char *ring = smem + SH::RING_OFF;
+  const int K = a.ring;
+  uint64_t *full = reinterpret_cast<uint64_t *>(ring + (size_t)K * UNIT);
+  uint64_t *empty = full + K;
+  int *hist = reinterpret_cast<int *>(empty + K);
+  const bool smem_hist = a.n_hist > 0 && a.n_hist <= kStagedHistMax;
+  const int C = a.n_channels;
+  const long long N = a.n_events;
+
+  if (threadIdx.x == 0) {
+    *s_abort = 0;
+    for (int k = 0; k < K; ++k) {
+      tc::mbar_init(&full[k], 1);
+      tc::mbar_init(&empty[k], SH::CONSUMERS);
+    }
+    tc::fence_mbarrier_init();
+    tc::fence_proxy_async_smem();
+  }
+  if (smem_hist)
+    for (int h = threadIdx.x; h < 2 * a.n_hist; h += blockDim.x) hist[h] = 0;
+  __syncthreads();
+
+  if (threadIdx.x >= SH::CONSUMERS) {
+    // ------------------------------------------------------------ producer
+    if (threadIdx.x == SH::CONSUMERS) {
+      const long long units_total =
+          ((a.couple_end - a.couple_begin - blockIdx.x + gridDim.x - 1) / gridDim.x) * C * 8;
+      cur->w = a.couple_begin + blockIdx.x;
+      cur->c = 0;
+      cur->r = 0;
+      staged_decode(a, T, cur->w, cur->i, cur->j0);
+      int slot = 0;
+      uint32_t phase = 0;
+      for (long long u = 0; u < units_total; ++u) {
+        if (u >= K) staged_wait(&empty[slot], phase ^ 1u, s_abort, a.error_flag);
+        if (*s_abort) break;
+        staged_issue<P, NWARP, ST>(a, &jmap, cur, ring + (size_t)slot * UNIT, &full[slot]);
+        if (++slot == K) {
+          slot = 0;
+          phase ^= 1u;
+        }
+      }
+    }
+  } else {
+    // ---------------------------------------------------------- FFT groups
+    const int g = threadIdx.x / G;
+    const int t = threadIdx.x % G;
+    float2 *buf = bufs + g * padded_len<P>();
+    unsigned *red = reds + g * NW * 8;
+    TwiddleRoots<P, 1> roots;
+    roots.load(t, a.twiddles);
+    const int ca = (t == 0) ? 0 : t;
+    const int cb = (t == 0) ? S / 2 : S - t;
+    int slot = 0;
+    uint32_t phase = 0;
+    for (long long w = a.couple_begin + blockIdx.x; w < a.couple_end; w += gridDim.x) {
+      long long i, j0;
+      staged_decode(a, T, w, i, j0);
+      long long ja = j0 + 2 * g, jb = ja + 1;
+      bool live, out_b;
+      if (!a.rect) {
+        const bool v1 = i < N && ja < N && ja >= i;
+        const bool v2 = i < N && jb < N && jb >= i;
+        live = v1 || v2;
+        out_b = v1 && v2;
+        if (!v1) ja = jb;
+        if (jb >= N) jb = ja;
+      } else {
+        live = ja - a.col_begin < a.n_cols;
+        out_b = jb - a.col_begin < a.n_cols;
+        if (!out_b) jb = ja;
+      }
+      const int ra = (1 + (int)(ja - j0)) * S, rb = (1 + (int)(jb - j0)) * S;  // rows of ja, jb in a unit
+      CoupleAcc y;
+      y.zero();
+      for (int c = 0; c < C; ++c) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          staged_wait(&full[slot], phase, s_abort, a.error_flag);
+          const ST_T *u = reinterpret_cast<const ST_T *>(ring + (size_t)slot * UNIT);
+          if (live) y.add<ST>(r, u[ca], u[ra + ca], u[rb + ca], u[cb], u[ra + cb], u[rb + cb]);
+          tc::mbar_arrive(&empty[slot]);
+          if (++slot == K) {
+            slot = 0;
+            phase ^= 1u;
+          }
+        }
+      }
+      if (live) {  // uniform over the group
+        float2 v[32];
+        assemble_couple(y, t, v);
+        inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots);
+        scan_and_write<P>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist);
+      }
+    }
+  }
+  __syncthreads();
+  if (smem_hist) {
+    for (int h = threadIdx.x; h < a.n_hist; h += blockDim.x) {
+      if (hist[h]) atomicAdd(&a.max_hist[h], hist[h]);
+      if (hist[a.n_hist + h]) atomicAdd(&a.min_hist[h], hist[a.n_hist + h]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host
+static bool staged_disabled() {
+  const char *e = getenv("SEISMIC_PAIR_KERNEL");
+  return e && strcmp(e, "direct") == 0;
+}
+static bool staged_forced() {
+  const char *e = getenv("SEISMIC_PAIR_KERNEL");
+  return e && strcmp(e, "staged") == 0;
+}
+
+constexpr int kStagedWarps = 12;  // FFT warps per CTA, plus the producer warp
+
+// The staged form serves P = 4096, where the three rows of a couple (3 x
+// C x 16 KB) outgrow L1 and the direct form waits on L2; for P <= 2048 the
+// direct form's 16 FFT warps per SM win (SEISMIC_PAIR_KERNEL=staged forces
+// the staged form for P = 512 .. 2048).
+bool staged_supported(int P, const PairArgs &a) {
+  if (P < 512 || P > 4096 || staged_disabled()) return false;
+  if (P < 4096 && !staged_forced()) return false;
+  if (a.stype < 0 || a.stype > 2) return false;
+  if ((reinterpret_cast<uintptr_t>(a.spectra) & 15u) != 0) return false;
+  if (a.rect && (reinterpret_cast<uintptr_t>(a.spectra_q) & 15u) != 0) return false;
+  return tensor_map_encoder() != nullptr;
+}
+
+long long staged_items_total(int P, const PairArgs &a) {
+  const long long T = 2 * (kStagedWarps * 32 / (P / 32));
+  if (a.rect) return a.n_query * ((a.n_cols + T - 1) / T);
+  const long long nb = (a.n_events + T - 1) / T;
+  return T * (nb * (nb + 1) / 2);
+}
+
+template <int P, int NWARP, int ST>
+static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_t s) {
+  using SH = Staged<P, NWARP>;
+  using ST_T = typename SpecT<ST>::T;
+  PairArgs a = a0;
+  const size_t unit = SH::template unit_bytes<ST>();
+  const size_t hist_reserve = (size_t)2 * kStagedHistMax * sizeof(int);
+  int K = (int)((kStagedSmemBudget - SH::RING_OFF - hist_reserve) / (unit + 2 * sizeof(uint64_t)));
+  if (K > kStagedRingMax) K = kStagedRingMax;
+  if (K < 2) return cudaErrorInvalidConfiguration;
+  a.ring = K;
+  const size_t hist_bytes = (a.n_hist > 0 && a.n_hist <= kStagedHistMax) ? (size_t)2 * a.n_hist * sizeof(int) : 0;
+  const size_t smem = SH::RING_OFF + (size_t)K * unit + (size_t)2 * K * sizeof(uint64_t) + hist_bytes;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(staged_pair_kernel<P, NWARP, ST>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmemBudget);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  // L2 band: about 48 MB of j spectra per band.
+  const long long ev_bytes = (long long)a.n_channels * (P / 2) * (long long)sizeof(ST_T);
+  const long long band_events = (48ll << 20) / (ev_bytes > 0 ? ev_bytes : 1);
+  a.band_tiles = (int)(band_events / SH::T > 1 ? band_events / SH::T : 1);
+
+  // Tensor map of the j spectra: dims {P/2 bins, C channels, N events},
+  // box {S bins, 1 channel, T events}.
+  CUtensorMap map;
+  const cuuint64_t dims[3] = {(cuuint64_t)(P / 2), (cuuint64_t)a.n_channels, (cuuint64_t)a.n_events};
+  const cuuint64_t strides[2] = {(cuuint64_t)(P / 2) * sizeof(ST_T),
+                                 (cuuint64_t)a.n_channels * (P / 2) * sizeof(ST_T)};
+  const cuuint32_t box[3] = {(cuuint32_t)SH::S, 1u, (cuuint32_t)SH::T};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUtensorMapDataType dt = sizeof(ST_T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  if (tensor_map_encoder()(&map, dt, 3, const_cast<void *>(a.spectra), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorInvalidValue;
+  const long long items = a.couple_end - a.couple_begin;
+  if (items <= 0) return cudaSuccess;
+  const int grid = (int)(items < sm_count ? items : sm_count);
+  staged_pair_kernel<P, NWARP, ST><<<grid, SH::THREADS, smem, s>>>(a, map);
+  return cudaGetLastError();
+}
+
+template <int P> static cudaError_t launch_staged_p(const PairArgs &a, int sm_count, cudaStream_t s) {
+  switch (a.stype) {
+    case 0: return launch_staged_t<P, kStagedWarps, 0>(a, sm_count, s);
+    case 1: return launch_staged_t<P, kStagedWarps, 1>(a, sm_count, s);
+    case 2: return launch_staged_t<P, kStagedWarps, 2>(a, sm_count, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_pairs_staged(int P, const PairArgs &a, int sm_count, cudaStream_t s) {
+  switch (P) {
+    case 512: return launch_staged_p<512>(a, sm_count, s);
+    case 1024: return launch_staged_p<1024>(a, sm_count, s);
+    case 2048: return launch_staged_p<2048>(a, sm_count, s);
+    case 4096: return launch_staged_p<4096>(a, sm_count, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace seismic

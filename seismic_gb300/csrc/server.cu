@@ -145,6 +145,7 @@ struct seismic_server {
   double *cat_norms = nullptr;
   int sm_count = 0;
   const float2 *tw = nullptr;
+  int *error_flag = nullptr;  // device flag set by a bounded wait that ran out
   int max_query = 64;
   // pool
   char *pool = nullptr;
@@ -283,12 +284,10 @@ int launch_request(seismic_server *s, Request *r) {
   pa.lags_neg = d_ln;
   pa.tile = 8;
   pa.twiddles = s->tw;
+  pa.error_flag = s->error_flag;
   pa.couple_begin = 0;
-  pa.couple_end = rect_couples_total(nq, r->n_cols, pa.tile);
-  const int ng = groups_per_cta(s->P);
-  long long grid = std::min<long long>((long long)s->sm_count * pair_ctas_per_sm(s->P), (pa.couple_end + ng - 1) / ng);
-  if (grid < 1) grid = 1;
-  if (e == cudaSuccess) e = launch_pairs(s->P, pa, (int)grid, st);
+  pa.couple_end = pair_work_total(s->P, pa);
+  if (e == cudaSuccess) e = launch_pair_work(s->P, pa, s->sm_count, 0, st);
   if (e == cudaSuccess && s->topk > 0) {
     topk_kernel<<<nq, kTopKThreads, 0, st>>>(d_vp, r->n_cols, s->topk, r->col_begin, d_tv, d_ti);
     e = cudaGetLastError();
@@ -389,6 +388,7 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   s->topk = topk;
   s->sm_count = sm;
   s->tw = tw;
+  s->error_flag = ef;
   s->max_query = max_query_events;
   const long long rows = n_catalog * n_channels;
   float *d_cat = nullptr;

@@ -143,7 +143,8 @@ def test_device_api_torch_stream_and_workspace(cuda_ok):
         xcorr.xcorr(t, 200, workspace=small)
 
 
-def test_pair_ranges_on_streams_compose_the_triangle(cuda_ok):
+@pytest.mark.parametrize("n,length,shift", [(150, 700, 300), (70, 2048, 2048)])  # direct form, staged form
+def test_pair_ranges_on_streams_compose_the_triangle(cuda_ok, n, length, shift):
     """Disjoint work-item ranges (how ranks or streams share one catalog)
     write exactly what one full launch writes."""
     import ctypes
@@ -151,9 +152,9 @@ def test_pair_ranges_on_streams_compose_the_triangle(cuda_ok):
     from seismic_gb300 import _lib
     from seismic_gb300.shard import couple_range
     lib = _lib.lib()
-    ev = synth.family_catalog(150, 3, 700, n_families=5, seed=91)
+    ev = synth.family_catalog(n, 3, length, n_families=5, seed=91)
     n, c, length = ev.shape
-    p = xcorr.resolve_padded_size(length, 300)
+    p = xcorr.resolve_padded_size(length, shift)
     t = torch.from_numpy(ev).cuda()
     rows = n * c
     spec = torch.empty(rows * p // 2 * 2, device="cuda")
@@ -165,18 +166,48 @@ def test_pair_ranges_on_streams_compose_the_triangle(cuda_ok):
             torch.zeros(m, device="cuda"), torch.zeros(m, dtype=torch.int32, device="cuda")]
     parts = [torch.full((m,), float("nan"), device="cuda"), torch.zeros(m, dtype=torch.int32, device="cuda"),
              torch.full((m,), float("nan"), device="cuda"), torch.zeros(m, dtype=torch.int32, device="cuda")]
-    _lib.check(lib.seismic_pairs_device(spec.data_ptr(), norms.data_ptr(), n, c, p, 1, 300, 0.0, 0, 0,
+    _lib.check(lib.seismic_pairs_device(spec.data_ptr(), norms.data_ptr(), n, c, p, 1, shift, 0.0, 0, 0,
                                         *(x.data_ptr() for x in full), None, None, None))
     total = lib.seismic_pair_couples(n, p, c)
     streams = [torch.cuda.Stream() for _ in range(3)]
     for r, s in enumerate(streams):
         b, e = couple_range(total, 3, r)
-        _lib.check(lib.seismic_pairs_device_range(spec.data_ptr(), norms.data_ptr(), n, c, p, 1, 300, 0.0, 0, b, e,
+        _lib.check(lib.seismic_pairs_device_range(spec.data_ptr(), norms.data_ptr(), n, c, p, 1, shift, 0.0, 0, b, e,
                                                   *(x.data_ptr() for x in parts), None, None,
                                                   ctypes.c_void_p(s.cuda_stream)))
     torch.cuda.synchronize()
     for a, b in zip(full, parts):
         assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("n,c,length,shift", [
+    (150, 3, 700, 300),    # P = 1024, ragged last tile
+    (61, 1, 2048, 2048),   # P = 4096
+    (130, 3, 2048, 1500),  # P = 4096, three channels
+    (200, 2, 300, 44),     # P = 512
+    (77, 3, 1024, 256),    # P = 2048, the serving shape
+])
+def test_staged_and_direct_forms_agree_bitwise(cuda_ok, monkeypatch, n, c, length, shift):
+    """The TMA-staged pair form and the direct-load form compute the same
+    couples (i; j, j+1), j even, in the same arithmetic order: identical
+    outputs and histograms, both within the FP64 bar."""
+    import torch
+    ev = synth.family_catalog(n, c, length, n_families=max(1, n // 10), seed=n + c)
+    t = torch.from_numpy(ev).cuda()
+    i, j = O.triu_pairs(n)
+    ref = O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(length, shift))
+    got = {}
+    for kind in ("staged", "direct"):
+        monkeypatch.setenv("SEISMIC_PAIR_KERNEL", kind)
+        r = xcorr.xcorr(t, shift, threshold=0.0, n_classes_hist=16)
+        torch.cuda.synchronize()
+        got[kind] = [x.cpu().numpy() for x in (r.vals_pos, r.lags_pos, r.vals_neg, r.lags_neg)] + \
+                    [r.max_hist.cpu().numpy(), r.min_hist.cpu().numpy()]
+        ag = O.agreement(*got[kind][:4], ref)
+        assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, (kind, ag)
+        assert ag.lag_mismatch == 0, (kind, ag)
+    for a, b in zip(got["staged"], got["direct"]):
+        np.testing.assert_array_equal(a, b)
 
 
 def test_precision_workload_size_properties(cuda_ok):

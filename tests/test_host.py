@@ -106,6 +106,54 @@ def test_scheduler_covers_triangle_exactly_once(n, tile):
     assert len(seen) == len(set(seen)) == n * (n + 1) // 2
 
 
+def _staged_decode(w, n, t, band):
+    """Python restatement of staged_decode (pairs_staged.cu), triangle mode:
+    item w -> (i, j0) with tiles of t x t events walked in column bands of
+    `band` tiles."""
+    nb = (n + t - 1) // t
+    x, ii = divmod(w, t)
+    band = band if band > 0 else nb
+    b0 = 0
+    while True:
+        be = min(b0 + band, nb)
+        wb = be - b0
+        cnt = b0 * wb + wb * (wb + 1) // 2
+        if x < cnt or be >= nb:
+            if x < b0 * wb:
+                bi, bj = divmod(x, wb)
+                bj += b0
+            else:
+                xx = x - b0 * wb
+                r = 0
+                while (r + 1) * wb - (r + 1) * r // 2 <= xx:
+                    r += 1
+                bi, bj = b0 + r, b0 + r + (xx - (r * wb - r * (r - 1) // 2))
+            return bi * t + ii, bj * t
+        x -= cnt
+        b0 = be
+
+
+def _staged_pairs(n, t, band, begin=0, end=None):
+    """Pairs written by items [begin, end) of the staged form (group g takes
+    j0 + 2g and j0 + 2g + 1; t = 2 * groups)."""
+    nb = (n + t - 1) // t
+    end = t * nb * (nb + 1) // 2 if end is None else end
+    seen = []
+    for w in range(begin, end):
+        i, j0 = _staged_decode(w, n, t, band)
+        for j in range(j0, j0 + t):
+            if i < n and j < n and j >= i:
+                seen.append((i, j))
+    return seen
+
+
+@pytest.mark.parametrize("n,t,band", [(1, 6, 0), (5, 6, 0), (37, 6, 0), (37, 6, 2), (100, 12, 1), (100, 12, 3),
+                                      (97, 24, 2), (300, 48, 2), (61, 6, 4)])
+def test_staged_scheduler_covers_triangle_exactly_once(n, t, band):
+    seen = _staged_pairs(n, t, band)
+    assert len(seen) == len(set(seen)) == n * (n + 1) // 2
+
+
 def test_native_api_rejects_bad_sizes_without_gpu(built_lib):
     """Argument validation runs before any CUDA call."""
     st = built_lib.seismic_xcorr_host(ctypes.c_void_p(1), 4, 1, 100, 100, 100, 96, 10, 0.0, 0, 0,
