@@ -211,16 +211,18 @@ long long pair_work_total(int P, const PairArgs &a) {
 cudaError_t launch_pair_work(int P, const PairArgs &a, int sm_count, int ctas_per_sm, cudaStream_t stream) {
   if (a.couple_end <= a.couple_begin) return cudaSuccess;
   if (staged_supported(P, a)) return launch_pairs_staged(P, a, sm_count, stream);
+  PairArgs d = a;  // direct form: L2 column bands of tiles (triangle mode)
+  if (!d.rect && d.band_tiles == 0) d.band_tiles = l2_band_tiles(d.n_channels, P, d.stype ? 4 : 8, d.tile);
   static int ctas_cache[16] = {0};
   const int lp2 = 31 - __builtin_clz((unsigned)P);
   if (!ctas_cache[lp2]) ctas_cache[lp2] = pair_ctas_per_sm(P);
   const int ctas = (ctas_per_sm > 0 && ctas_per_sm < ctas_cache[lp2]) ? ctas_per_sm : ctas_cache[lp2];
   const int NG = groups_per_cta(P);
-  long long want = (a.couple_end - a.couple_begin + NG - 1) / NG;
+  long long want = (d.couple_end - d.couple_begin + NG - 1) / NG;
   long long grid = (long long)sm_count * ctas;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
-  return launch_pairs(P, a, (int)grid, stream);
+  return launch_pairs(P, d, (int)grid, stream);
 }
 
 int device_context(int *sm_count, const float2 **twiddles, int **error_flag) {

@@ -83,6 +83,14 @@ struct PairArgs {
   int *error_flag;
 };
 
+// Tile columns per L2 band of the triangle walk (PairArgs::band_tiles) so
+// that one band of j spectra takes about 48 MB of L2.
+inline int l2_band_tiles(long long n_channels, int P, int elem_bytes, int tile) {
+  const long long ev_bytes = n_channels * (P / 2) * (long long)elem_bytes;
+  const long long band_events = (48ll << 20) / (ev_bytes > 0 ? ev_bytes : 1);
+  return (int)(band_events / tile > 1 ? band_events / tile : 1);
+}
+
 // ---- staged pair form (pairs_staged.cu): spectra staged into shared memory
 // by TMA (P = 4096 by default).  Work items are (event i, T consecutive j).
 bool staged_supported(int P, const PairArgs &a);

@@ -51,6 +51,42 @@ __device__ __forceinline__ void decode_tile(long long x, long long nb, long long
   bj = b + (x - tri_start(b, nb));
 }
 
+// Tile x of the upper triangle of nb x nb tiles in column-band order: bands
+// of `band` tile columns (band <= 0: one band, i.e. plain row-major), each
+// walked row by row from the top row down to its own diagonal, so the
+// columns of one band stay in L2 while every row above it passes over them.
+__host__ __device__ __forceinline__ void band_tile(long long x, long long nb, long long band, long long &bi,
+                                                   long long &bj) {
+  if (band <= 0 || band > nb) band = nb;
+  long long b0 = 0;  // first tile column of the band
+  for (;;) {
+    const long long be = b0 + band < nb ? b0 + band : nb;
+    const long long wb = be - b0;
+    const long long cnt = b0 * wb + wb * (wb + 1) / 2;
+    if (x < cnt || be >= nb) {
+      if (x < b0 * wb) {  // rows above the band: full width
+        bi = x / wb;
+        bj = b0 + (x - bi * wb);
+      } else {            // the band's own triangle
+        long long r, c;
+#ifdef __CUDA_ARCH__
+        decode_tile(x - b0 * wb, wb, r, c);
+#else
+        const long long xx = x - b0 * wb;
+        r = 0;
+        while (tri_start(r + 1, wb) <= xx) ++r;
+        c = r + (xx - tri_start(r, wb));
+#endif
+        bi = b0 + r;
+        bj = b0 + c;
+      }
+      return;
+    }
+    x -= cnt;
+    b0 = be;
+  }
+}
+
 // Spectrum storage types: 0 float2 (FP32 form), 1 half2, 2 bfloat162.  For
 // the half types the pointwise product a * conj(b) runs in the storage type
 // (HMUL2) and is accumulated over channels in FP32.

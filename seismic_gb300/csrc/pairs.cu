@@ -11,8 +11,8 @@
 // or product spectrum ever written to global memory.
 //
 // Work decomposition.  Events are cut into square tiles of `tile` events;
-// tiles (bi, bj >= bi) are enumerated row-major over the upper triangle
-// (decode_tile).  A tile holds tile*tile/2 couples (pair_core.cuh); couples
+// tiles (bi, bj >= bi) of the upper triangle are enumerated in column bands
+// of `band_tiles` tiles (band_tile; 0 = plain row-major).  A tile holds tile*tile/2 couples (pair_core.cuh); couples
 // are dealt to groups of G = P/32 threads round-robin, the groups of one CTA
 // taking neighbouring couples of the same tile, whose spectra they read
 // straight from global memory (L2).  This form serves every size P and the
@@ -111,7 +111,7 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
       const long long tile = w / cpt;
       const long long lc = w - tile * cpt;
       long long bi, bj;
-      decode_tile(tile, nb, bi, bj);
+      band_tile(tile, nb, a.band_tiles, bi, bj);
       const long long ii = (2 * lc) / T, jj = (2 * lc) % T;
       i = bi * T + ii;
       const long long j1 = bj * T + jj, j2 = j1 + 1;

@@ -43,7 +43,7 @@ constexpr int kStagedHistMax = 1024;  // larger histograms use global atomics
 constexpr int kStagedRingMax = 16;
 constexpr size_t kStagedSmemBudget = 227 * 1024;
 
-template <int P, int NWARP> struct Staged {
+template <int P, int NWARP, int RU> struct Staged {  // RU: chunks r per ring slot
   static constexpr int G = P / 32;
   static constexpr int NG = NWARP * 32 / G;  // FFT groups per CTA
   static constexpr int T = 2 * NG;           // j events per item = tile side; T items per tile
@@ -56,9 +56,9 @@ template <int P, int NWARP> struct Staged {
   static constexpr size_t RED_BYTES = (size_t)NG * NW * 8 * sizeof(unsigned);
   static constexpr size_t PROD_OFF = (EX_BYTES + RED_BYTES + 15) / 16 * 16;
   static constexpr size_t RING_OFF = (PROD_OFF + 64 + 127) / 128 * 128;
-  template <int ST> static constexpr size_t unit_bytes() {
-    return (size_t)ROWS * S * sizeof(typename SpecT<ST>::T);
-  }
+  // one chunk r of every staged row, and a ring slot of RU chunks
+  template <int ST> static constexpr size_t sub_bytes() { return (size_t)ROWS * S * sizeof(typename SpecT<ST>::T); }
+  template <int ST> static constexpr size_t unit_bytes() { return RU * sub_bytes<ST>(); }
 };
 
 // Item w -> (i, j0).  Triangle: tile x = w / T in band order, i = bi T + w % T.
@@ -71,42 +71,15 @@ __host__ __device__ __forceinline__ void staged_decode(const PairArgs &a, int T,
     return;
   }
   const long long nb = (a.n_events + T - 1) / T;
-  long long x = w / T;
-  const long long ii = w - x * T;
-  const long long band = a.band_tiles > 0 ? a.band_tiles : nb;
-  long long b0 = 0;  // first tile column of the band
-  for (;;) {
-    const long long be = b0 + band < nb ? b0 + band : nb;
-    const long long wb = be - b0;
-    const long long cnt = b0 * wb + wb * (wb + 1) / 2;
-    if (x < cnt || be >= nb) {
-      long long bi, bj;
-      if (x < b0 * wb) {  // rows above the band: full width
-        bi = x / wb;
-        bj = b0 + (x - bi * wb);
-      } else {            // the band's own triangle
-        long long r, c;
-#ifdef __CUDA_ARCH__
-        decode_tile(x - b0 * wb, wb, r, c);
-#else
-        const long long xx = x - b0 * wb;
-        r = 0;
-        while (tri_start(r + 1, wb) <= xx) ++r;
-        c = r + (xx - tri_start(r, wb));
-#endif
-        bi = b0 + r;
-        bj = b0 + c;
-      }
-      i = bi * T + ii;
-      j0 = bj * T;
-      return;
-    }
-    x -= cnt;
-    b0 = be;
-  }
+  const long long x = w / T;
+  long long bi, bj;
+  band_tile(x, nb, a.band_tiles, bi, bj);
+  i = bi * T + (w - x * T);
+  j0 = bj * T;
 }
 
 __device__ __forceinline__ void staged_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err) {
+  if (tc::mbar_try_wait(bar, parity)) return;  // the common case: already complete
   if (*abort_flag) {
     (void)tc::mbar_try_wait(bar, parity);
     return;
@@ -123,10 +96,10 @@ struct StagedCursor {
   int c, r;
 };
 
-template <int P, int NWARP, int ST>
+template <int P, int NWARP, int RU, int ST>
 __device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMap *jmap, StagedCursor *cur,
                                              unsigned char *dst, uint64_t *full) {
-  using SH = Staged<P, NWARP>;
+  using SH = Staged<P, NWARP, RU>;
   using ST_T = typename SpecT<ST>::T;
   constexpr int S = SH::S, H = P / 2;
   constexpr uint32_t CHUNK = (uint32_t)(S * sizeof(ST_T));
@@ -136,9 +109,14 @@ __device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMa
   const long long i = cur->i < n_i ? cur->i : n_i - 1;  // ragged last tile row: staged but unused
   const int c = cur->c, r = cur->r;
   tc::mbar_arrive_expect_tx(full, (uint32_t)SH::template unit_bytes<ST>());
-  tc::bulk_load(dst, spec_i + (i * C + c) * (long long)H + r * S, CHUNK, full);
-  tc::tma_load_3d(dst + CHUNK, jmap, r * S, c, (int)cur->j0, full);
-  if (++cur->r == 8) {
+#pragma unroll
+  for (int h = 0; h < RU; ++h) {
+    unsigned char *d = dst + h * SH::template sub_bytes<ST>();
+    tc::bulk_load(d, spec_i + (i * C + c) * (long long)H + (r + h) * S, CHUNK, full);
+    tc::tma_load_3d(d + CHUNK, jmap, (r + h) * S, c, (int)cur->j0, full);
+  }
+  cur->r += RU;
+  if (cur->r == 8) {
     cur->r = 0;
     if (++cur->c == C) {
       cur->c = 0;
@@ -148,10 +126,10 @@ __device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMa
   }
 }
 
-template <int P, int NWARP, int ST>
+template <int P, int NWARP, int RU, int ST>
 __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
     staged_pair_kernel(const PairArgs a, const __grid_constant__ CUtensorMap jmap) {
-  using SH = Staged<P, NWARP>;
+  using SH = Staged<P, NWARP, RU>;
   using ST_T = typename SpecT<ST>::T;
   constexpr int G = SH::G, T = SH::T, S = SH::S, NW = SH::NW;
   constexpr uint32_t UNIT = (uint32_t)SH::template unit_bytes<ST>();
@@ -187,7 +165,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
     // ------------------------------------------------------------ producer
     if (threadIdx.x == SH::CONSUMERS) {
       const long long units_total =
-          ((a.couple_end - a.couple_begin - blockIdx.x + gridDim.x - 1) / gridDim.x) * C * 8;
+          ((a.couple_end - a.couple_begin - blockIdx.x + gridDim.x - 1) / gridDim.x) * C * (8 / RU);
       cur->w = a.couple_begin + blockIdx.x;
       cur->c = 0;
       cur->r = 0;
@@ -197,7 +175,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       for (long long u = 0; u < units_total; ++u) {
         if (u >= K) staged_wait(&empty[slot], phase ^ 1u, s_abort, a.error_flag);
         if (*s_abort) break;
-        staged_issue<P, NWARP, ST>(a, &jmap, cur, ring + (size_t)slot * UNIT, &full[slot]);
+        staged_issue<P, NWARP, RU, ST>(a, &jmap, cur, ring + (size_t)slot * UNIT, &full[slot]);
         if (++slot == K) {
           slot = 0;
           phase ^= 1u;
@@ -238,10 +216,14 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       y.zero();
       for (int c = 0; c < C; ++c) {
 #pragma unroll
-        for (int r = 0; r < 8; ++r) {
+        for (int rp = 0; rp < 8; rp += RU) {
           staged_wait(&full[slot], phase, s_abort, a.error_flag);
           const ST_T *u = reinterpret_cast<const ST_T *>(ring + (size_t)slot * UNIT);
-          if (live) y.add<ST>(r, u[ca], u[ra + ca], u[rb + ca], u[cb], u[ra + cb], u[rb + cb]);
+#pragma unroll
+          for (int h = 0; h < RU; ++h) {
+            const ST_T *uh = u + h * (SH::ROWS * S);
+            if (live) y.add<ST>(rp + h, uh[ca], uh[ra + ca], uh[rb + ca], uh[cb], uh[ra + cb], uh[rb + cb]);
+          }
           tc::mbar_arrive(&empty[slot]);
           if (++slot == K) {
             slot = 0;
@@ -278,13 +260,21 @@ static bool staged_forced() {
 
 constexpr int kStagedWarps = 12;  // FFT warps per CTA, plus the producer warp
 
-// The staged form serves P = 4096, where the three rows of a couple (3 x
-// C x 16 KB) outgrow L1 and the direct form waits on L2; for P <= 2048 the
-// direct form's 16 FFT warps per SM win (SEISMIC_PAIR_KERNEL=staged forces
-// the staged form for P = 512 .. 2048).
+// Chunks per ring slot: 4 (half the slot waits and releases of 2, a ring of
+// two to four slots), or 2 for FP32 spectra when SEISMIC_STAGED_RU=2.
+static int staged_ru() {
+  const char *e = getenv("SEISMIC_STAGED_RU");
+  return (e && strcmp(e, "2") == 0) ? 2 : 4;
+}
+
+// The staged form serves P = 4096, and P = 2048 with several channels, where
+// the three rows of a couple (3 x C x 4P bytes) outgrow L1 and the direct
+// form waits on L2; for single-channel P <= 2048 the direct form's 16 FFT
+// warps per SM win (SEISMIC_PAIR_KERNEL=staged forces the staged form for
+// P = 512 .. 2048, =direct the direct form everywhere).
 bool staged_supported(int P, const PairArgs &a) {
   if (P < 512 || P > 4096 || staged_disabled()) return false;
-  if (P < 4096 && !staged_forced()) return false;
+  if (!staged_forced() && !(P == 4096 || (P == 2048 && a.n_channels > 1))) return false;
   if (a.stype < 0 || a.stype > 2) return false;
   if ((reinterpret_cast<uintptr_t>(a.spectra) & 15u) != 0) return false;
   if (a.rect && (reinterpret_cast<uintptr_t>(a.spectra_q) & 15u) != 0) return false;
@@ -298,9 +288,9 @@ long long staged_items_total(int P, const PairArgs &a) {
   return T * (nb * (nb + 1) / 2);
 }
 
-template <int P, int NWARP, int ST>
+template <int P, int NWARP, int RU, int ST>
 static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_t s) {
-  using SH = Staged<P, NWARP>;
+  using SH = Staged<P, NWARP, RU>;
   using ST_T = typename SpecT<ST>::T;
   PairArgs a = a0;
   const size_t unit = SH::template unit_bytes<ST>();
@@ -313,15 +303,12 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
   const size_t smem = SH::RING_OFF + (size_t)K * unit + (size_t)2 * K * sizeof(uint64_t) + hist_bytes;
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(staged_pair_kernel<P, NWARP, ST>,
+    cudaError_t e = cudaFuncSetAttribute(staged_pair_kernel<P, NWARP, RU, ST>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmemBudget);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  // L2 band: about 48 MB of j spectra per band.
-  const long long ev_bytes = (long long)a.n_channels * (P / 2) * (long long)sizeof(ST_T);
-  const long long band_events = (48ll << 20) / (ev_bytes > 0 ? ev_bytes : 1);
-  a.band_tiles = (int)(band_events / SH::T > 1 ? band_events / SH::T : 1);
+  a.band_tiles = l2_band_tiles(a.n_channels, P, (int)sizeof(ST_T), SH::T);
 
   // Tensor map of the j spectra: dims {P/2 bins, C channels, N events},
   // box {S bins, 1 channel, T events}.
@@ -339,15 +326,17 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
   const long long items = a.couple_end - a.couple_begin;
   if (items <= 0) return cudaSuccess;
   const int grid = (int)(items < sm_count ? items : sm_count);
-  staged_pair_kernel<P, NWARP, ST><<<grid, SH::THREADS, smem, s>>>(a, map);
+  staged_pair_kernel<P, NWARP, RU, ST><<<grid, SH::THREADS, smem, s>>>(a, map);
   return cudaGetLastError();
 }
 
 template <int P> static cudaError_t launch_staged_p(const PairArgs &a, int sm_count, cudaStream_t s) {
   switch (a.stype) {
-    case 0: return launch_staged_t<P, kStagedWarps, 0>(a, sm_count, s);
-    case 1: return launch_staged_t<P, kStagedWarps, 1>(a, sm_count, s);
-    case 2: return launch_staged_t<P, kStagedWarps, 2>(a, sm_count, s);
+    case 0:
+      return staged_ru() == 2 ? launch_staged_t<P, kStagedWarps, 2, 0>(a, sm_count, s)
+                              : launch_staged_t<P, kStagedWarps, 4, 0>(a, sm_count, s);
+    case 1: return launch_staged_t<P, kStagedWarps, 4, 1>(a, sm_count, s);
+    case 2: return launch_staged_t<P, kStagedWarps, 4, 2>(a, sm_count, s);
     default: return cudaErrorInvalidValue;
   }
 }

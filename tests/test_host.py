@@ -69,50 +69,11 @@ def test_packed_index():
     assert xcorr.packed_index(big - 1, big - 1, big) == big * (big + 1) // 2 - 1
 
 
-def _scheduler_pairs(n, tile):
-    """Python restatement of the pair kernel's work decomposition
-    (decode_tile + couple split in pairs.cu) to check coverage."""
-    nb = (n + tile - 1) // tile
-    return _scheduler_pairs_range(n, tile, 0, nb * (nb + 1) // 2 * (tile * tile // 2))
-
-
-def _scheduler_pairs_range(n, tile, begin, end):
-    """Pairs produced by work items [begin, end) of the triangle of n events."""
-    nb = (n + tile - 1) // tile
-    cpt = tile * tile // 2
-    seen = []
-    for w in range(begin, end):
-        tl, lc = divmod(w, cpt)
-        twonb1 = 2.0 * nb + 1.0
-        b = int((twonb1 - np.sqrt(twonb1 * twonb1 - 8.0 * tl)) * 0.5)
-        b = min(max(b, 0), nb - 1)
-        start = lambda q: q * nb - q * (q - 1) // 2  # noqa: E731
-        while b + 1 < nb and start(b + 1) <= tl:
-            b += 1
-        while b > 0 and start(b) > tl:
-            b -= 1
-        bi, bj = b, b + (tl - start(b))
-        ii, jj = divmod(2 * lc, tile)
-        i = bi * tile + ii
-        for j in (bj * tile + jj, bj * tile + jj + 1):
-            if i < n and j < n and j >= i:
-                seen.append((i, j))
-    return seen
-
-
-@pytest.mark.parametrize("n,tile", [(1, 8), (2, 8), (13, 8), (37, 4), (64, 8), (9, 2), (50, 2)])
-def test_scheduler_covers_triangle_exactly_once(n, tile):
-    seen = _scheduler_pairs(n, tile)
-    assert len(seen) == len(set(seen)) == n * (n + 1) // 2
-
-
-def _staged_decode(w, n, t, band):
-    """Python restatement of staged_decode (pairs_staged.cu), triangle mode:
-    item w -> (i, j0) with tiles of t x t events walked in column bands of
-    `band` tiles."""
-    nb = (n + t - 1) // t
-    x, ii = divmod(w, t)
-    band = band if band > 0 else nb
+def _band_tile(x, nb, band):
+    """Python restatement of band_tile (pair_core.cuh): tile x of the upper
+    triangle of nb x nb tiles in column bands of `band` tiles (0 = one band,
+    plain row-major)."""
+    band = band if 0 < band <= nb else nb
     b0 = 0
     while True:
         be = min(b0 + band, nb)
@@ -121,26 +82,56 @@ def _staged_decode(w, n, t, band):
         if x < cnt or be >= nb:
             if x < b0 * wb:
                 bi, bj = divmod(x, wb)
-                bj += b0
-            else:
-                xx = x - b0 * wb
-                r = 0
-                while (r + 1) * wb - (r + 1) * r // 2 <= xx:
-                    r += 1
-                bi, bj = b0 + r, b0 + r + (xx - (r * wb - r * (r - 1) // 2))
-            return bi * t + ii, bj * t
+                return bi, bj + b0
+            xx = x - b0 * wb
+            r = 0
+            while (r + 1) * wb - (r + 1) * r // 2 <= xx:
+                r += 1
+            return b0 + r, b0 + r + (xx - (r * wb - r * (r - 1) // 2))
         x -= cnt
         b0 = be
 
 
+def _scheduler_pairs(n, tile, band=0):
+    """Python restatement of the direct pair kernel's work decomposition
+    (band_tile + couple split in pairs.cu) to check coverage."""
+    nb = (n + tile - 1) // tile
+    return _scheduler_pairs_range(n, tile, 0, nb * (nb + 1) // 2 * (tile * tile // 2), band)
+
+
+def _scheduler_pairs_range(n, tile, begin, end, band=0):
+    """Pairs produced by work items [begin, end) of the triangle of n events."""
+    nb = (n + tile - 1) // tile
+    cpt = tile * tile // 2
+    seen = []
+    for w in range(begin, end):
+        tl, lc = divmod(w, cpt)
+        bi, bj = _band_tile(tl, nb, band)
+        ii, jj = divmod(2 * lc, tile)
+        i = bi * tile + ii
+        for j in (bj * tile + jj, bj * tile + jj + 1):
+            if i < n and j < n and j >= i:
+                seen.append((i, j))
+    return seen
+
+
+@pytest.mark.parametrize("n,tile,band", [(1, 8, 0), (2, 8, 0), (13, 8, 0), (37, 4, 0), (64, 8, 0), (9, 2, 0),
+                                         (50, 2, 0), (37, 4, 3), (64, 8, 1), (50, 2, 7)])
+def test_scheduler_covers_triangle_exactly_once(n, tile, band):
+    seen = _scheduler_pairs(n, tile, band)
+    assert len(seen) == len(set(seen)) == n * (n + 1) // 2
+
+
 def _staged_pairs(n, t, band, begin=0, end=None):
-    """Pairs written by items [begin, end) of the staged form (group g takes
-    j0 + 2g and j0 + 2g + 1; t = 2 * groups)."""
+    """Pairs written by items [begin, end) of the staged form (pairs_staged.cu):
+    item w is tile w // t in band order and its row w % t; group g takes
+    j0 + 2g and j0 + 2g + 1, t = 2 * groups."""
     nb = (n + t - 1) // t
     end = t * nb * (nb + 1) // 2 if end is None else end
     seen = []
     for w in range(begin, end):
-        i, j0 = _staged_decode(w, n, t, band)
+        bi, bj = _band_tile(w // t, nb, band)
+        i, j0 = bi * t + w % t, bj * t
         for j in range(j0, j0 + t):
             if i < n and j < n and j >= i:
                 seen.append((i, j))
