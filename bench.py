@@ -47,6 +47,15 @@ WORKLOAD_TEXT = {
 CPU_SAMPLE_EVENTS = {"scale": 640, "precision": 1024, "small": 200}
 
 
+def pair_kernel_name(p: int, c: int) -> str:
+    """The pair form the library dispatches for FP32 spectra of size p, c channels."""
+    if os.environ.get("SEISMIC_PAIR_KERNEL") == "direct":
+        return "pair_kernel (direct-load form)"
+    if p == 4096 or (p == 2048 and c > 1) or os.environ.get("SEISMIC_PAIR_KERNEL") == "staged":
+        return "staged_pair_kernel (TMA-staged form)"
+    return "pair_kernel (direct-load form)"
+
+
 def fft_flops_per_pair(p: int, c: int) -> float:
     """Algorithmic work per pair of the FFT form: one size-P inverse FFT
     (2.5 P log2 P) plus C conj-products of P/2+1 bins (6 flops each)."""
@@ -386,7 +395,7 @@ def run_ours(args):
         roofline = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
                     "frac": achieved_tf / peak_tf,
                     "traffic": (traffic_pp * npairs) if traffic_pp is not None else None,
-                    "kernel": "pair_kernel",
+                    "kernel": pair_kernel_name(p, c),
                     "peak_source": f"nominal FP32 FMA rate: {sm_count} SMs x 128 lanes x 2 flop x median SM clock "
                                    f"{sm_mhz:.0f} MHz under load (MEASURED_PEAKS.json has no FP32 figure)",
                     "work": f"{npairs} pairs x (2.5 P log2 P + 6 C (P/2+1)) flop, P={p}, C={c}",
