@@ -291,6 +291,36 @@ int seismic_server_stats(seismic_server *server, long long *completed, long long
 /* Waits for every admitted and pending request, then frees everything. */
 int seismic_server_destroy(seismic_server *server);
 
+/* ---- consumers of the packed outputs --------------------------------------
+ *
+ * Sparse output.  Replaces the host-side sparsification of the reference's
+ * driver (Correlation_in_OMP/test_c.py:43-55: each packed array becomes a
+ * 1 x N(N+1)/2 scipy CSR matrix of its nonzeros, saved with save_npz), on the
+ * device and in one pass over the outputs.  Keeps, in packed order, every pair
+ * with d_vals_pos > threshold (index, value, lag into the *_pos arrays) and
+ * every pair with d_vals_neg < -threshold (into the *_neg arrays).  Applied to
+ * outputs computed with threshold 0 it gives exactly the entries the
+ * reference's matrices hold after a run with `threshold` (the pair kernel
+ * thresholds with the same strict comparisons).  Writes at most `capacity`
+ * entries per side and the full counts to d_counts[0] (positive side) and
+ * d_counts[1] (negative side); capacity 0 only counts.  `workspace` holds
+ * seismic_compact_workspace_bytes(n_pairs) bytes.  Stream-ordered. */
+size_t seismic_compact_workspace_bytes(long long n_pairs);
+int seismic_compact_pairs_device(const float *d_vals_pos, const int *d_lags_pos, const float *d_vals_neg,
+                                 const int *d_lags_neg, long long n_pairs, float threshold, long long capacity,
+                                 long long *d_index_pos, float *d_value_pos, int *d_lag_pos,
+                                 long long *d_index_neg, float *d_value_neg, int *d_lag_neg,
+                                 long long *d_counts, void *workspace, size_t workspace_bytes, void *stream);
+
+/* Histograms of stored coefficients, accumulated into d_max_hist / d_min_hist
+ * with the rule of Correlation_in_OMP/correlation_c.cpp:116-117, :128-129
+ * (last bin for |v| >= 1, else int(|v| / float(1.0 / n_classes_hist))).  On
+ * outputs computed with threshold 0 it equals the pair kernel's own
+ * histograms, except that pairs with a zero-norm event (stored as 0) count in
+ * bin 0; it lets a threshold be chosen after the correlation has run. */
+int seismic_histogram_device(const float *d_vals_pos, const float *d_vals_neg, long long n_pairs,
+                             int n_classes_hist, int *d_max_hist, int *d_min_hist, void *stream);
+
 /* Number of kernels this library has launched in this process. */
 unsigned long long seismic_launch_count(void);
 

@@ -68,6 +68,10 @@ def _declare(lib):
                                                         ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                         ctypes.c_int, vp, vp, vp, vp, vp, vp, vp]),
         "seismic_noalloc_scratch_bytes": (ctypes.c_size_t, []),
+        "seismic_compact_workspace_bytes": (ctypes.c_size_t, [c_ll]),
+        "seismic_compact_pairs_device": (ctypes.c_int, [vp, vp, vp, vp, c_ll, ctypes.c_float, c_ll,
+                                                        vp, vp, vp, vp, vp, vp, vp, vp, ctypes.c_size_t, vp]),
+        "seismic_histogram_device": (ctypes.c_int, [vp, vp, c_ll, ctypes.c_int, vp, vp, vp]),
         "seismic_launch_count": (ctypes.c_ulonglong, []),
         "seismic_release_cached_memory": (ctypes.c_int, []),
     }
