@@ -155,7 +155,7 @@ TuneEntry tune_lookup(int P, int n_channels);
 // ---- lag-GEMM form (laggemm.cu): time-domain lag sums on tcgen05 tensor cores
 struct LagPlan {
   bool ok;
-  int lp, nt, wt, wpad, jp, nm, strip_bytes, xs_len, jc, stages, smem;
+  int lp, nt, wt, wpad, jp, nbuf, nm, strip_bytes, xs_len, jc, stages, smem;
 };
 LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int n_hist);
 size_t lag_workspace_bytes(long long n_events, int n_channels, int length);

@@ -20,13 +20,17 @@
 //
 // Work: persistent CTAs (one per SM: 512 TMEM columns and ~200 KB of shared
 // memory each) walk items (I-block of 128 events, chunk of `jc` events j >=
-// block start); j's are processed `jp` at a time (TMEM holds jp
-// accumulators of nt * wt columns).  Warp roles:
-//   warps 0-3  build the Hankel strips of the next j's, then read TMEM
-//              (lane = event i) and reduce max/min + lags, write outputs;
+// block start); j's are processed `jp` at a time (a "pass": jp accumulators
+// of nt * wt columns).  The stages overlap: the Hankel strips are double
+// buffered per (pass, channel) and TMEM holds two passes' accumulators when
+// 2 jp wpad <= 512, so the strips of the next j are built and the previous
+// pass's accumulators are reduced while the tensor cores run.  Warp roles:
+//   warps 0-3  build the Hankel strips of the next (pass, channel);
 //   warp 4     TMA producer of the A tiles (128 events x 64 samples, hi and
 //              lo, 128-byte swizzle) into a `stages`-deep ring;
-//   warp 5     TMEM allocation and the single MMA-issuing thread.
+//   warp 5     TMEM allocation and the single MMA-issuing thread;
+//   warps 6-9  epilogue: read TMEM (one lane quarter each, lane = event i),
+//              reduce max/min + lags, write outputs.
 // All mbarrier waits are bounded; a wait that runs out raises the shared
 // abort flag and the device error flag, every role then unwinds, the CTA
 // frees its TMEM and exits.
@@ -49,7 +53,7 @@ using tc::smem_u32;
 
 constexpr int kLagM = 128;       // events per I-block (MMA M)
 constexpr int kLagKC = 64;       // samples per A tile (one 128-byte swizzle row)
-constexpr int kLagThreads = 192; // 6 warps
+constexpr int kLagThreads = 320; // 10 warps
 constexpr int kLagHistMax = 1024;
 
 // ------------------------------------------------------------------ prep
@@ -96,7 +100,8 @@ struct LagArgs {
   int shift;      // lags d = 1-shift .. shift
   int wpad;       // 2*shift rounded up to a multiple of 16*nt
   int nt, wt;     // N-tiles per j and their width (wt * nt == wpad)
-  int jp;         // j's per pass (TMEM: jp * wpad <= 512 columns)
+  int jp;         // j's per pass (TMEM: nbuf * jp * wpad <= 512 columns)
+  int nbuf;       // TMEM accumulator buffers (2 when they fit, else 1)
   int jc;         // j's per work item (multiple of jp)
   int nm;         // core matrices per Hankel strip = wpad/8 + lp/8 - 1
   int strip_bytes;
@@ -125,14 +130,14 @@ static LagSmem lag_smem_layout(const LagArgs &a) {
   s.a = off;
   off += a.stages * 2 * kLagM * kLagKC * 2;  // hi + lo tiles per stage
   s.hank = off;
-  off += a.jp * 2 * a.strip_bytes;
+  off += 2 * a.jp * 2 * a.strip_bytes;  // two buffers of jp (hi, lo) strips
   s.xs = off;
   off += a.jp * 2 * ((a.xs_len * 2 + 15) / 16 * 16);
   s.hist = off;
   off += (a.n_hist > 0 && a.n_hist <= kLagHistMax) ? 2 * a.n_hist * 4 : 0;
   off = (off + 7) / 8 * 8;
   s.bars = off;
-  off += (2 * a.stages + 5) * 8;
+  off += (2 * a.stages + 9) * 8;
   s.misc = off;
   off += 16;
   s.total = off + 1024;  // room to align the base
@@ -185,8 +190,8 @@ __global__ void __launch_bounds__(kLagThreads, 1)
   } L = {a.off_a, a.off_hank, a.off_xs, a.off_hist, a.off_bars, a.off_misc};
   uint64_t *bars = reinterpret_cast<uint64_t *>(base + L.bars);
   uint64_t *a_full = bars, *a_empty = bars + a.stages;
-  uint64_t *hank_full = bars + 2 * a.stages, *hank_empty = hank_full + 1, *tmem_full = hank_full + 2,
-           *tmem_empty = hank_full + 3, *mma_drain = hank_full + 4;
+  uint64_t *hank_full = bars + 2 * a.stages, *hank_empty = hank_full + 2, *tmem_full = hank_full + 4,
+           *tmem_empty = hank_full + 6, *mma_drain = hank_full + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(base + L.misc);
   volatile int *abort_flag = reinterpret_cast<volatile int *>(base + L.misc + 4);
   int *hist = reinterpret_cast<int *>(base + L.hist);
@@ -199,10 +204,12 @@ __global__ void __launch_bounds__(kLagThreads, 1)
       tc::mbar_init(&a_full[s], 1);
       tc::mbar_init(&a_empty[s], 1);
     }
-    tc::mbar_init(hank_full, kLagM);
-    tc::mbar_init(hank_empty, 1);
-    tc::mbar_init(tmem_full, 1);
-    tc::mbar_init(tmem_empty, kLagM);
+    for (int k = 0; k < 2; ++k) {
+      tc::mbar_init(&hank_full[k], kLagM);  // the 128 builder threads
+      tc::mbar_init(&hank_empty[k], 1);     // MMA commit
+      tc::mbar_init(&tmem_full[k], 1);      // MMA commit
+      tc::mbar_init(&tmem_empty[k], kLagM); // the 128 epilogue threads
+    }
     tc::mbar_init(mma_drain, 1);
     *abort_flag = 0;
     tc::fence_mbarrier_init();
@@ -224,6 +231,7 @@ __global__ void __launch_bounds__(kLagThreads, 1)
   const int C = a.C;
   const uint32_t tile_bytes = kLagM * kLagKC * 2;
   const uint32_t idesc = tc::idesc_bf16_f32(kLagM, a.wt);
+  const uint32_t buf_cols = (uint32_t)(a.jp * a.wpad);  // TMEM columns of one pass
 
   long long b = 0, q = 0;
   advance_item(b, q, blockIdx.x, N, a.jc, nblk);
@@ -265,20 +273,21 @@ __global__ void __launch_bounds__(kLagThreads, 1)
     // ================================================= MMA issuer
     if (lane == 0) {
       int stage = 0;
-      uint32_t phase = 0, hank_phase = 0, tmem_phase = 0;
-      bool first_pass = true;
+      uint32_t phase = 0;
+      long long unit = 0, pass = 0;  // (pass, channel) strip units; passes
       for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk)) {
         const long long j_begin = bb * kLagM + qq * a.jc;
         const long long j_end = min(j_begin + a.jc, N);
-        for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp) {
+        for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp, ++pass) {
           const int njp = (int)min((long long)a.jp, j_end - j0);
-          if (!first_pass && !lag_wait(tmem_empty, tmem_phase, abort_flag, a.error_flag)) break;
-          if (!first_pass) tmem_phase ^= 1;
-          first_pass = false;
+          const int tb = (int)(pass % a.nbuf);
+          const long long tuse = pass / a.nbuf;
+          if (tuse > 0 && !lag_wait(&tmem_empty[tb], (uint32_t)((tuse - 1) & 1), abort_flag, a.error_flag)) break;
           tc::fence_after_sync();
-          for (int c = 0; c < C && !*abort_flag; ++c) {
-            if (!lag_wait(hank_full, hank_phase, abort_flag, a.error_flag)) break;
-            hank_phase ^= 1;
+          const uint32_t tbase = tmem + (uint32_t)tb * buf_cols;
+          for (int c = 0; c < C && !*abort_flag; ++c, ++unit) {
+            const int hb = (int)(unit & 1);
+            if (!lag_wait(&hank_full[hb], (uint32_t)((unit >> 1) & 1), abort_flag, a.error_flag)) break;
             tc::fence_after_sync();
             for (int kc = 0; kc < kchunks; ++kc) {
               if (!lag_wait(&a_full[stage], phase, abort_flag, a.error_flag)) break;
@@ -291,13 +300,13 @@ __global__ void __launch_bounds__(kLagThreads, 1)
                 const uint64_t dal = tc::smem_desc(a_lo + 32 * ks, 16, 1024, 2);
                 const int h0 = kc * (kLagKC / 8) + 2 * ks;  // k core-matrix index
                 for (int p = 0; p < njp; ++p) {
-                  const uint32_t s_hi = smem_u32(base + L.hank + (p * 2 + 0) * a.strip_bytes);
+                  const uint32_t s_hi = smem_u32(base + L.hank + ((hb * a.jp + p) * 2 + 0) * a.strip_bytes);
                   const uint32_t s_lo = s_hi + a.strip_bytes;
                   for (int nt = 0; nt < a.nt; ++nt) {
                     const uint32_t coff = (uint32_t)((nt * (a.wt / 8) + h0) * 128);
                     const uint64_t dbh = tc::smem_desc(s_hi + coff, 128, 128, 0);
                     const uint64_t dbl = tc::smem_desc(s_lo + coff, 128, 128, 0);
-                    const uint32_t d = tmem + (uint32_t)(p * a.wpad + nt * a.wt);
+                    const uint32_t d = tbase + (uint32_t)(p * a.wpad + nt * a.wt);
                     const uint32_t acc0 = (c > 0 || kc > 0 || ks > 0) ? 1u : 0u;
                     tc::mma_bf16(d, dah, dbh, idesc, acc0);
                     tc::mma_bf16(d, dah, dbl, idesc, 1u);
@@ -311,32 +320,29 @@ __global__ void __launch_bounds__(kLagThreads, 1)
                 phase ^= 1;
               }
             }
-            tc::mma_commit(hank_empty);  // Hankel strips of channel c no longer read
+            tc::mma_commit(&hank_empty[hb]);  // this unit's strips are no longer read
           }
-          tc::mma_commit(tmem_full);
+          tc::mma_commit(&tmem_full[tb]);
         }
       }
       // every issued MMA has finished before TMEM is freed (bounded)
       tc::mma_commit(mma_drain);
       tc::mbar_wait(mma_drain, 0, 1u << 20);
     }
-  } else {
-    // ================================================= builders + epilogue (warps 0-3)
-    const int e_lane = tid;  // 0..127 : TMEM lane = event within the block
-    uint32_t hank_phase = 0, tmem_phase = 0;
-    bool first = true;
+  } else if (warp < 4) {
+    // ================================================= Hankel strip builders (warps 0-3)
+    const int e_lane = tid;  // 0..127
+    long long unit = 0;
     for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk)) {
       const long long j_begin = bb * kLagM + qq * a.jc;
       const long long j_end = min(j_begin + a.jc, N);
       for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp) {
         const int njp = (int)min((long long)a.jp, j_end - j0);
-        for (int c = 0; c < C && !*abort_flag; ++c) {
-          // ---- wait until the previous strips are no longer read, then build
-          if (!first) {
-            if (!lag_wait(hank_empty, hank_phase, abort_flag, a.error_flag)) break;
-            hank_phase ^= 1;
-          }
-          first = false;
+        for (int c = 0; c < C && !*abort_flag; ++c, ++unit) {
+          const int hb = (int)(unit & 1);
+          // wait until the MMAs of the unit two back (same buffer) no longer read it
+          if (unit >= 2 && !lag_wait(&hank_empty[hb], (uint32_t)(((unit >> 1) - 1) & 1), abort_flag, a.error_flag))
+            break;
           const int xs_stride = (a.xs_len * 2 + 15) / 16 * 16;
           for (int p = 0; p < njp; ++p) {
             const long long j = j0 + p;
@@ -359,7 +365,8 @@ __global__ void __launch_bounds__(kLagThreads, 1)
             for (int hl = 0; hl < 2; ++hl) {
               const unsigned short *xs =
                   reinterpret_cast<const unsigned short *>(base + L.xs + (p * 2 + hl) * xs_stride);
-              uint4 *strip = reinterpret_cast<uint4 *>(base + L.hank + (p * 2 + hl) * a.strip_bytes);
+              uint4 *strip =
+                  reinterpret_cast<uint4 *>(base + L.hank + ((hb * a.jp + p) * 2 + hl) * a.strip_bytes);
               // core matrix m, row r = xs[8m + r .. 8m + r + 7]
               for (int rowi = e_lane; rowi < a.nm * 8; rowi += kLagM) {
                 const int o = rowi;  // 8m + r
@@ -371,30 +378,55 @@ __global__ void __launch_bounds__(kLagThreads, 1)
               }
             }
           }
+          asm volatile("bar.sync 1, 128;" ::: "memory");  // xs is rewritten by the next unit
           tc::fence_proxy_async_smem();
-          tc::mbar_arrive(hank_full);
+          tc::mbar_arrive(&hank_full[hb]);
         }
-        if (*abort_flag) break;
-        // ---- epilogue: TMEM rows -> max / min and lags
-        if (!lag_wait(tmem_full, tmem_phase, abort_flag, a.error_flag)) break;
-        tmem_phase ^= 1;
+      }
+    }
+  } else {
+    // ================================================= epilogue (warps 6-9)
+    const int quarter = warp & 3;                 // TMEM lanes 32 quarter .. 32 quarter + 31
+    const int e_lane = 32 * quarter + lane;       // event within the block
+    const uint32_t lane_addr = (uint32_t)(32 * quarter) << 16;
+    long long pass = 0;
+    for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk)) {
+      const long long j_begin = bb * kLagM + qq * a.jc;
+      const long long j_end = min(j_begin + a.jc, N);
+      for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp, ++pass) {
+        const int njp = (int)min((long long)a.jp, j_end - j0);
+        const int tb = (int)(pass % a.nbuf);
+        if (!lag_wait(&tmem_full[tb], (uint32_t)((pass / a.nbuf) & 1), abort_flag, a.error_flag)) break;
         tc::fence_after_sync();
         const long long i = bb * kLagM + e_lane;
         for (int p = 0; p < njp; ++p) {
           const long long j = j0 + p;
           float best = 0.f, worst = 0.f;
           int bn = 0, wn = 0;
-          for (int c0 = 0; c0 < a.wpad; c0 += 16) {
-            float v[16];
-            tc::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(p * a.wpad + c0), v);
+          const uint32_t col0 = (uint32_t)tb * buf_cols + (uint32_t)(p * a.wpad);
+          for (int c0 = 0; c0 < a.wpad; c0 += 64) {
+            // up to four 16-column loads in flight, one wait
+            uint32_t r[4][16];
+            const int nl = min(4, (a.wpad - c0) / 16);
 #pragma unroll
-            for (int k = 0; k < 16; ++k) {
-              const int n = c0 + k;
-              if (n < 2 * a.shift) {
-                // n increasing = lag decreasing: ">=" keeps the largest n among
-                // equal values, i.e. the smallest lag (first occurrence)
-                if (v[k] >= best) { best = v[k]; bn = n; }
-                if (v[k] <= worst) { worst = v[k]; wn = n; }
+            for (int h = 0; h < 4; ++h)
+              if (h < nl) tc::tmem_ld16_issue(tmem + lane_addr + col0 + (uint32_t)(c0 + 16 * h), r[h]);
+            tc::tmem_ld_wait();
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+              if (h < nl) {
+                tc::tmem_regs_ready(r[h]);
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                  const int n = c0 + 16 * h + k;
+                  const float v = __uint_as_float(r[h][k]);
+                  if (n < 2 * a.shift) {
+                    // n increasing = lag decreasing: ">=" keeps the largest n among
+                    // equal values, i.e. the smallest lag (first occurrence)
+                    if (v >= best) { best = v; bn = n; }
+                    if (v <= worst) { worst = v; wn = n; }
+                  }
+                }
               }
             }
           }
@@ -440,7 +472,7 @@ __global__ void __launch_bounds__(kLagThreads, 1)
           }
         }
         tc::fence_before_sync();
-        tc::mbar_arrive(tmem_empty);
+        tc::mbar_arrive(&tmem_empty[tb]);
       }
     }
   }
@@ -491,7 +523,9 @@ LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int 
   pl.nt = w > 256 ? 2 : 1;
   pl.wt = ((w + pl.nt - 1) / pl.nt + 15) / 16 * 16;
   pl.wpad = pl.nt * pl.wt;
-  pl.jp = 512 / pl.wpad >= 2 ? 2 : 1;
+  // two TMEM buffers of jp accumulators when they fit in 512 columns
+  pl.nbuf = 2 * pl.wpad <= 512 ? 2 : 1;
+  pl.jp = 512 / pl.nbuf / pl.wpad >= 2 ? 2 : 1;
   pl.nm = pl.wpad / 8 + pl.lp / 8 - 1;
   pl.strip_bytes = (pl.nm + 1) * 128;
   pl.xs_len = pl.wpad + pl.lp + 16;
@@ -552,6 +586,7 @@ cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length,
   a.nt = pl.nt;
   a.wt = pl.wt;
   a.jp = pl.jp;
+  a.nbuf = pl.nbuf;
   a.jc = pl.jc;
   a.nm = pl.nm;
   a.strip_bytes = pl.strip_bytes;
