@@ -219,11 +219,14 @@ template <int G> __device__ __forceinline__ void group_sync(int group_in_cta) {
 template <int P, int R> __device__ __forceinline__ void pass_read(const float2 *buf, float2 (&v)[32], int t) {
   constexpr int G = P / 32;
   constexpr int J = 32 / R;
+  // pad16(j + c) = pad16(j) + 17 c / 16 for c a multiple of 16: one padded
+  // base per job, constant offsets for its R values
+  static_assert((P / R) % 16 == 0, "pass_read: stride must be a multiple of 16");
 #pragma unroll
   for (int q = 0; q < J; ++q) {
-    const int j = t + q * G;
+    const float2 *row = buf + pad16(t + q * G);
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[q * R + r] = buf[pad16(j + r * (P / R))];
+    for (int r = 0; r < R; ++r) v[q * R + r] = row[r * (P / R) * 17 / 16];
   }
 }
 
@@ -249,9 +252,10 @@ template <int P, int R, int NS> __device__ __forceinline__ void pass_write(float
 #pragma unroll
   for (int q = 0; q < J; ++q) {
     const int j = t + q * G;
-    const int base = (j / NS) * NS * R + (j % NS);
+    static_assert(NS % 16 == 0, "pass_write: stride must be a multiple of 16");
+    float2 *row = buf + pad16((j / NS) * NS * R + (j % NS));  // constant offsets below
 #pragma unroll
-    for (int r = 0; r < R; ++r) buf[pad16(base + r * NS)] = v[q * R + r];
+    for (int r = 0; r < R; ++r) row[r * NS * 17 / 16] = v[q * R + r];
   }
 }
 

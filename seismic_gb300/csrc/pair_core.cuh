@@ -65,7 +65,8 @@ __host__ __device__ __forceinline__ void band_tile(long long x, long long nb, lo
     const long long cnt = b0 * wb + wb * (wb + 1) / 2;
     if (x < cnt || be >= nb) {
       if (x < b0 * wb) {  // rows above the band: full width
-        bi = x / wb;
+        // 32-bit division when it fits (a 64-bit one is a long software routine)
+        bi = (x < 0x7fffffffLL && wb < 0x7fffffffLL) ? (long long)((unsigned)x / (unsigned)wb) : x / wb;
         bj = b0 + (x - bi * wb);
       } else {            // the band's own triangle
         long long r, c;

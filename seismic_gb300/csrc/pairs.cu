@@ -108,11 +108,12 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
     long long i, ja, jb;
     bool out_b;
     if (!a.rect) {
-      const long long tile = w / cpt;
-      const long long lc = w - tile * cpt;
+      // 32-bit division where it fits (a 64-bit one is a long software routine)
+      const long long tile = w < 0x7fffffffLL ? (long long)((unsigned)w / (unsigned)cpt) : w / cpt;
+      const int lc2 = (int)(2 * (w - tile * cpt));
       long long bi, bj;
       band_tile(tile, nb, a.band_tiles, bi, bj);
-      const long long ii = (2 * lc) / T, jj = (2 * lc) % T;
+      const long long ii = lc2 / (int)T, jj = lc2 - (int)ii * (int)T;
       i = bi * T + ii;
       const long long j1 = bj * T + jj, j2 = j1 + 1;
       const bool v1 = i < N && j1 < N && j1 >= i;
@@ -124,8 +125,10 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
     } else {
       // chunk of T couple-columns x all queries; j are subset columns
       const long long per_chunk = a.n_query * T;
-      const long long chunk = w / per_chunk, r = w - chunk * per_chunk;
-      i = r / T;
+      const long long chunk = (w < 0x7fffffffLL && per_chunk < 0x7fffffffLL)
+                                  ? (long long)((unsigned)w / (unsigned)per_chunk) : w / per_chunk;
+      const long long r = w - chunk * per_chunk;
+      i = r < 0x7fffffffLL ? (long long)((unsigned)r / (unsigned)T) : r / T;
       const long long j1 = 2 * (chunk * T + (r - i * T)), j2 = j1 + 1;
       if (j1 >= a.n_cols) continue;  // uniform over the group
       out_b = j2 < a.n_cols;

@@ -41,6 +41,10 @@ namespace seismic {
 
 constexpr int kStagedHistMax = 1024;  // larger histograms use global atomics
 constexpr int kStagedRingMax = 16;
+// Decoded items published by the producer; it runs at most kStagedRingMax
+// units (>= 2 per item) ahead of the slowest FFT thread, so 16 entries never
+// wrap onto an item still being read.
+constexpr int kItemRing = 16;
 constexpr size_t kStagedSmemBudget = 227 * 1024;
 
 template <int P, int NWARP, int RU> struct Staged {  // RU: chunks r per ring slot
@@ -55,7 +59,9 @@ template <int P, int NWARP, int RU> struct Staged {  // RU: chunks r per ring sl
   static constexpr size_t EX_BYTES = (size_t)NG * padded_len<P>() * sizeof(float2);
   static constexpr size_t RED_BYTES = (size_t)NG * NW * 8 * sizeof(unsigned);
   static constexpr size_t PROD_OFF = (EX_BYTES + RED_BYTES + 15) / 16 * 16;
-  static constexpr size_t RING_OFF = (PROD_OFF + 64 + 127) / 128 * 128;
+  // producer area: cursor (48 B), abort flag, item ring of kItemRing (i, j0)
+  static constexpr size_t ITEMS_OFF = PROD_OFF + 64;
+  static constexpr size_t RING_OFF = (ITEMS_OFF + kItemRing * 16 + 127) / 128 * 128;
   // one chunk r of every staged row, and a ring slot of RU chunks
   template <int ST> static constexpr size_t sub_bytes() { return (size_t)ROWS * S * sizeof(typename SpecT<ST>::T); }
   template <int ST> static constexpr size_t unit_bytes() { return RU * sub_bytes<ST>(); }
@@ -65,7 +71,8 @@ template <int P, int NWARP, int RU> struct Staged {  // RU: chunks r per ring sl
 __host__ __device__ __forceinline__ void staged_decode(const PairArgs &a, int T, long long w, long long &i,
                                                        long long &j0) {
   if (a.rect) {
-    const long long blk = w / a.n_query;
+    const long long blk = (w < 0x7fffffffLL && a.n_query < 0x7fffffffLL)
+                              ? (long long)((unsigned)w / (unsigned)a.n_query) : w / a.n_query;
     i = w - blk * a.n_query;
     j0 = a.col_begin + blk * T;
     return;
@@ -94,11 +101,15 @@ __device__ __forceinline__ void staged_wait(uint64_t *bar, uint32_t parity, vola
 struct StagedCursor {
   long long w, i, j0;
   int c, r;
+  unsigned seq;  // items decoded so far by this CTA
+};
+struct StagedItem {
+  long long i, j0;
 };
 
 template <int P, int NWARP, int RU, int ST>
 __device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMap *jmap, StagedCursor *cur,
-                                             unsigned char *dst, uint64_t *full) {
+                                             StagedItem *items, unsigned char *dst, uint64_t *full) {
   using SH = Staged<P, NWARP, RU>;
   using ST_T = typename SpecT<ST>::T;
   constexpr int S = SH::S, H = P / 2;
@@ -121,7 +132,12 @@ __device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMa
     if (++cur->c == C) {
       cur->c = 0;
       cur->w += gridDim.x;
-      if (cur->w < a.couple_end) staged_decode(a, SH::T, cur->w, cur->i, cur->j0);
+      if (cur->w < a.couple_end) {
+        staged_decode(a, SH::T, cur->w, cur->i, cur->j0);
+        // published before the item's first unit is armed: that arrive
+        // releases it to the FFT threads that wait on the unit
+        items[++cur->seq % kItemRing] = StagedItem{cur->i, cur->j0};
+      }
     }
   }
 }
@@ -139,6 +155,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
   unsigned *reds = reinterpret_cast<unsigned *>(smem + SH::EX_BYTES);
   StagedCursor *cur = reinterpret_cast<StagedCursor *>(smem + SH::PROD_OFF);
   volatile int *s_abort = reinterpret_cast<volatile int *>(smem + SH::PROD_OFF + 48);
+  StagedItem *items = reinterpret_cast<StagedItem *>(smem + SH::ITEMS_OFF);
   unsigned char *ring = smem + SH::RING_OFF;
   const int K = a.ring;
   uint64_t *full = reinterpret_cast<uint64_t *>(ring + (size_t)K * UNIT);
@@ -170,12 +187,14 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       cur->c = 0;
       cur->r = 0;
       staged_decode(a, T, cur->w, cur->i, cur->j0);
+      cur->seq = 0;
+      items[0] = StagedItem{cur->i, cur->j0};
       int slot = 0;
       uint32_t phase = 0;
       for (long long u = 0; u < units_total; ++u) {
         if (u >= K) staged_wait(&empty[slot], phase ^ 1u, s_abort, a.error_flag);
         if (*s_abort) break;
-        staged_issue<P, NWARP, RU, ST>(a, &jmap, cur, ring + (size_t)slot * UNIT, &full[slot]);
+        staged_issue<P, NWARP, RU, ST>(a, &jmap, cur, items, ring + (size_t)slot * UNIT, &full[slot]);
         if (++slot == K) {
           slot = 0;
           phase ^= 1u;
@@ -194,9 +213,12 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
     const int cb = (t == 0) ? S / 2 : S - t;
     int slot = 0;
     uint32_t phase = 0;
-    for (long long w = a.couple_begin + blockIdx.x; w < a.couple_end; w += gridDim.x) {
-      long long i, j0;
-      staged_decode(a, T, w, i, j0);
+    unsigned seq = 0;
+    for (long long w = a.couple_begin + blockIdx.x; w < a.couple_end; w += gridDim.x, ++seq) {
+      // the item's first unit being full also publishes its (i, j0)
+      staged_wait(&full[slot], phase, s_abort, a.error_flag);
+      const StagedItem it = items[seq % kItemRing];
+      const long long i = it.i, j0 = it.j0;
       long long ja = j0 + 2 * g, jb = ja + 1;
       bool live, out_b;
       if (!a.rect) {
@@ -267,14 +289,14 @@ static int staged_ru() {
   return (e && strcmp(e, "2") == 0) ? 2 : 4;
 }
 
-// The staged form serves P = 4096, and P = 2048 with several channels, where
-// the three rows of a couple (3 x C x 4P bytes) outgrow L1 and the direct
-// form waits on L2; for single-channel P <= 2048 the direct form's 16 FFT
-// warps per SM win (SEISMIC_PAIR_KERNEL=staged forces the staged form for
-// P = 512 .. 2048, =direct the direct form everywhere).
+// The staged form serves P = 2048 and 4096, where the three rows of a couple
+// (3 x C x 4P bytes) outgrow L1 and the direct form waits on L2; for smaller
+// P the direct form's 16 FFT warps per SM are kept (SEISMIC_PAIR_KERNEL=staged
+// forces the staged form for P = 512 and 1024, =direct the direct form
+// everywhere).
 bool staged_supported(int P, const PairArgs &a) {
   if (P < 512 || P > 4096 || staged_disabled()) return false;
-  if (!staged_forced() && !(P == 4096 || (P == 2048 && a.n_channels > 1))) return false;
+  if (!staged_forced() && P < 2048) return false;
   if (a.stype < 0 || a.stype > 2) return false;
   if ((reinterpret_cast<uintptr_t>(a.spectra) & 15u) != 0) return false;
   if (a.rect && (reinterpret_cast<uintptr_t>(a.spectra_q) & 15u) != 0) return false;
