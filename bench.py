@@ -51,7 +51,7 @@ def pair_kernel_name(p: int, c: int) -> str:
     """The pair form the library dispatches for FP32 spectra of size p, c channels."""
     if os.environ.get("SEISMIC_PAIR_KERNEL") == "direct":
         return "pair_kernel (direct-load form)"
-    if p >= 2048 and p <= 4096 or os.environ.get("SEISMIC_PAIR_KERNEL") == "staged":
+    if 512 <= p <= 4096:
         return "staged_pair_kernel (TMA-staged form)"
     return "pair_kernel (direct-load form)"
 

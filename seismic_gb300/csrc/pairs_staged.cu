@@ -275,12 +275,25 @@ static bool staged_disabled() {
   const char *e = getenv("SEISMIC_PAIR_KERNEL");
   return e && strcmp(e, "direct") == 0;
 }
-static bool staged_forced() {
-  const char *e = getenv("SEISMIC_PAIR_KERNEL");
-  return e && strcmp(e, "staged") == 0;
-}
 
 constexpr int kStagedWarps = 12;  // FFT warps per CTA, plus the producer warp
+
+// The widest FFT-warp count whose CTA (plus the producer warp) still gets 128
+// registers a thread: at most 4 warps per SM sub-partition, i.e. 16 warps,
+// in whole groups of P/32 threads.
+constexpr int staged_wide_warps(int P) { return P >= 4096 ? 12 : (P == 2048 ? 14 : 15); }
+
+// FFT warps the dispatch uses.  The wide CTA (more FFT warps, a ring of
+// 2-chunk slots) wins where one channel's item fits its smaller ring: FP32
+// spectra, one channel, P = 2048 (263 vs 230 M pairs/s measured; with three
+// channels 175 vs 184).  SEISMIC_STAGED_WARPS=wide / =12 forces either.
+static int staged_nwarp(int P, int stype, int n_channels) {
+  if (stype != 0) return kStagedWarps;
+  const char *e = getenv("SEISMIC_STAGED_WARPS");
+  if (e && strcmp(e, "wide") == 0) return staged_wide_warps(P);
+  if (e && strcmp(e, "12") == 0) return kStagedWarps;
+  return (P == 2048 && n_channels == 1) ? staged_wide_warps(P) : kStagedWarps;
+}
 
 // Chunks per ring slot: 4 (half the slot waits and releases of 2, a ring of
 // two to four slots), or 2 for FP32 spectra when SEISMIC_STAGED_RU=2.
@@ -289,14 +302,13 @@ static int staged_ru() {
   return (e && strcmp(e, "2") == 0) ? 2 : 4;
 }
 
-// The staged form serves P = 2048 and 4096, where the three rows of a couple
-// (3 x C x 4P bytes) outgrow L1 and the direct form waits on L2; for smaller
-// P the direct form's 16 FFT warps per SM are kept (SEISMIC_PAIR_KERNEL=staged
-// forces the staged form for P = 512 and 1024, =direct the direct form
-// everywhere).
+// The staged form serves P = 512 .. 4096: there the three rows of a couple
+// (3 x C x 4P bytes) outgrow what L1 keeps and the direct form waits on L2
+// (measured, staged vs direct M pairs/s: P=512 C=1 973 vs 926, P=1024 C=1
+// 549 vs 496, C=3 379 vs 339).  SEISMIC_PAIR_KERNEL=direct forces the direct
+// form everywhere.
 bool staged_supported(int P, const PairArgs &a) {
   if (P < 512 || P > 4096 || staged_disabled()) return false;
-  if (!staged_forced() && P < 2048) return false;
   if (a.stype < 0 || a.stype > 2) return false;
   if ((reinterpret_cast<uintptr_t>(a.spectra) & 15u) != 0) return false;
   if (a.rect && (reinterpret_cast<uintptr_t>(a.spectra_q) & 15u) != 0) return false;
@@ -304,7 +316,7 @@ bool staged_supported(int P, const PairArgs &a) {
 }
 
 long long staged_items_total(int P, const PairArgs &a) {
-  const long long T = 2 * (kStagedWarps * 32 / (P / 32));
+  const long long T = 2 * (staged_nwarp(P, a.stype, a.n_channels) * 32 / (P / 32));
   if (a.rect) return a.n_query * ((a.n_cols + T - 1) / T);
   const long long nb = (a.n_events + T - 1) / T;
   return T * (nb * (nb + 1) / 2);
@@ -355,6 +367,8 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
 template <int P> static cudaError_t launch_staged_p(const PairArgs &a, int sm_count, cudaStream_t s) {
   switch (a.stype) {
     case 0:
+      // the wide CTA's exchange buffers leave room for a ring of 2-chunk slots
+      if (staged_nwarp(P, 0, a.n_channels) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 2, 0>(a, sm_count, s);
       return staged_ru() == 2 ? launch_staged_t<P, kStagedWarps, 2, 0>(a, sm_count, s)
                               : launch_staged_t<P, kStagedWarps, 4, 0>(a, sm_count, s);
     case 1: return launch_staged_t<P, kStagedWarps, 4, 1>(a, sm_count, s);

@@ -143,7 +143,7 @@ def test_device_api_torch_stream_and_workspace(cuda_ok):
         xcorr.xcorr(t, 200, workspace=small)
 
 
-@pytest.mark.parametrize("n,length,shift", [(150, 700, 300), (70, 2048, 2048)])  # direct form, staged form
+@pytest.mark.parametrize("n,length,shift", [(150, 200, 56), (70, 2048, 2048)])  # direct form (P=256), staged form
 def test_pair_ranges_on_streams_compose_the_triangle(cuda_ok, n, length, shift):
     """Disjoint work-item ranges (how ranks or streams share one catalog)
     write exactly what one full launch writes."""
@@ -186,6 +186,7 @@ def test_pair_ranges_on_streams_compose_the_triangle(cuda_ok, n, length, shift):
     (130, 3, 2048, 1500),  # P = 4096, three channels
     (200, 2, 300, 44),     # P = 512
     (77, 3, 1024, 256),    # P = 2048, the serving shape
+    (90, 1, 1024, 128),    # P = 2048, one channel: the wide (14 FFT warp) CTA
 ])
 def test_staged_and_direct_forms_agree_bitwise(cuda_ok, monkeypatch, n, c, length, shift):
     """The TMA-staged pair form and the direct-load form compute the same
