@@ -62,6 +62,10 @@ def fft_flops_per_pair(p: int, c: int) -> float:
     return 2.5 * p * np.log2(p) + 6.0 * c * (p // 2 + 1)
 
 
+# arithmetic type of each form's products (accumulation is FP32 in all of them)
+FORM_DTYPE = {"fp32": "f32", "fp16": "f16", "bf16": "bf16", "laggemm": "bf16x3 (hi+lo)", "laggemm16": "f16"}
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -286,7 +290,7 @@ def run_ours(args):
                                                 20, 0, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(), ln.data_ptr(),
                                                 hist[0].data_ptr(), hist[1].data_ptr(), sh))
     else:  # forms run as one call: spectra + pairs (fp16/bf16) or prep + lag-GEMM
-        wsb = lib.seismic_xcorr_workspace_bytes(n, c, length, shift, p if args.form != "laggemm" else 0, form_code)
+        wsb = lib.seismic_xcorr_workspace_bytes(n, c, length, shift, p if not args.form.startswith("laggemm") else 0, form_code)
         if wsb == 0:
             raise SystemExit(f"form {args.form} does not support this workload")
         lag_ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
@@ -296,7 +300,7 @@ def run_ours(args):
 
         def pairs_call():
             _lib.check(lib.seismic_xcorr_device(d_ev.data_ptr(), n, c, length, c * length, length,
-                                                p if args.form != "laggemm" else 0, shift, 0.0, 20,
+                                                p if not args.form.startswith("laggemm") else 0, shift, 0.0, 20,
                                                 form_code, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(),
                                                 ln.data_ptr(), hist[0].data_ptr(), hist[1].data_ptr(),
                                                 lag_ws.data_ptr(), wsb, sh))
@@ -386,7 +390,7 @@ def run_ours(args):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         peaks = {}
-    if args.form != "laggemm":  # FFT forms: pair kernel on the FP32 pipe
+    if not args.form.startswith("laggemm"):  # FFT forms: pair kernel on the FP32 pipe
         flops = npairs * fft_flops_per_pair(p, c)
         achieved_tf = flops / t_pair_mean / 1e12
         sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
@@ -410,8 +414,9 @@ def run_ours(args):
                     "kernel": "lag_gemm_kernel (+ lag_prep_kernel, < 1 % of the step)",
                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) of measured" if "bf16_tflops" in peaks
                     else "fallback 1.9 PFLOP/s",
-                    "work": f"{npairs} pairs x {c} ch x 2 L (2 shift) flop, L={length}, shift={shift}; the three "
-                            f"BF16 hi/lo products issue 3x this on the tensor pipe",
+                    "work": f"{npairs} pairs x {c} ch x 2 L (2 shift) flop, L={length}, shift={shift}; "
+                            + ("the three BF16 hi/lo products issue 3x this on the tensor pipe"
+                               if args.form == "laggemm" else "one FP16 product per lag sum"),
                     "pair_kernel_ms": t_pair_mean * 1e3, "pair_kernel_share_of_step": t_pair_mean / step_mean}
     spec_bytes = rows * (length * 4 + (p // 2) * 8 + 8)
     spectra_roof = None
@@ -425,7 +430,7 @@ def run_ours(args):
 
     out = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_mean * 1e3, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32",
+           "vs_baseline": None, "dtype": FORM_DTYPE.get(args.form, "f32"),
            "data": "synthetic: seeded family-based waveforms (no public dataset; the reference's is not distributed)",
            "config": {"workload": args.workload + ": " + WORKLOAD_TEXT[args.workload], "n_events": n,
                       "n_channels": c, "event_length": length, "shift": shift, "padded_size": p,
@@ -624,7 +629,7 @@ def run_serving(args):
                                 mp_context=mp.get_context("spawn")) as ex:
         cat = np.concatenate(list(ex.map(_serving_chunk, jobs)))
     shift = 256
-    form = args.form if args.form in ("fp32", "fp16") else "fp16"
+    form = args.form if args.form in ("fp32", "fp16", "laggemm", "laggemm16") else "fp16"
     lib = _lib.lib()
     srv = Server(cat, shift=shift, form=form, n_slots=4, max_query_events=64, topk=16)
     rng = np.random.default_rng(77)
@@ -635,6 +640,8 @@ def run_serving(args):
     for k in range(args.warmup):
         srv.wait(srv.submit(query(64, 100 + k)))
     # isolated latency: 64-event queries against the whole catalog, one at a time
+    clocks = ClockSampler(_gpu_id(torch.device("cuda", 0), 0))
+    clocks.start()
     launches0 = lib.seismic_launch_count()
     iso = []
     t0 = time.perf_counter()
@@ -673,6 +680,7 @@ def run_serving(args):
         levels.append({"offered_req_per_s": rate, "requests": n_req, "p50_ms": float(np.percentile(lat, 50)),
                        "p99_ms": float(np.percentile(lat, 99)), "pairs_per_s": pairs / wall})
     launches = lib.seismic_launch_count() - launches0
+    clk = clocks.stop()
     # FP64 check on a sample of one isolated request's pairs
     res = srv.wait(srv.submit(iso_q[0]))
     sel = rng.integers(0, n_cat, 400)
@@ -682,16 +690,18 @@ def run_serving(args):
     out = {"metric": METRIC + "; serving p50/p99 latency", "value": iso_pairs / iso_wall, "unit": "pairs/s",
            "n_gpus": 1, "steps": len(iso), "warmup": args.warmup,
            "ms_per_step": float(np.mean(iso)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f16" if form == "fp16" else "f32",
+           "dtype": FORM_DTYPE.get(form, "f32"),
            "data": "synthetic: seeded family-based waveforms (no public dataset; the reference's is not distributed)",
            "config": {"workload": "serving: 50,000-event resident catalog x 3 channels x L=1024, lags -255..256, "
-                                  f"{form} catalog spectra + FP64 norms on device, 4 request slots, top-16",
+                                  f"{form} catalog " + ("16-bit sample planes" if form.startswith("laggemm")
+                                                         else "spectra") + " + FP64 norms on device, 4 request "
+                                  "slots, top-16",
                       "n_catalog": n_cat},
            "serving": {"isolated_64_event_full_catalog": {"p50_ms": float(np.percentile(iso, 50)),
                                                           "p99_ms": float(np.percentile(iso, 99)),
                                                           "requests": len(iso), "pairs_per_request": 64 * n_cat},
                        "poisson_load": levels},
-           "fp64_error": fp, "gpu_launches": int(launches),
+           "fp64_error": fp, "clocks": clk, "gpu_launches": int(launches),
            "e2e": {"value": iso_pairs / iso_wall, "unit": "pairs/s",
                    "h2d_bytes_per_step": 64 * 3 * 1024 * 4, "d2h_bytes_per_step": 64 * n_cat * 16 + 64 * 16 * 12,
                    "entry_point": "seismic_server_submit/wait (C ABI), query in, all pair outputs + top-16 out"}}
@@ -743,7 +753,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOAD_TEXT), default="scale")
-    ap.add_argument("--form", choices=["fp32", "fp16", "bf16", "laggemm"], default="fp32",
+    ap.add_argument("--form", choices=["fp32", "fp16", "bf16", "laggemm", "laggemm16"], default="fp32",
                     help="fp32: fused FFT form; fp16/bf16: half-precision spectra and products; "
                          "laggemm: tensor-core lag-GEMM (short windows)")
     ap.add_argument("--skip-e2e", action="store_true")

@@ -71,6 +71,11 @@ extern "C" {
  * per-event lag strip to fit in shared memory (event_length up to ~1500 at
  * 2*shift = 256). */
 #define SEISMIC_FORM_LAGGEMM_BF16X3 2
+/* The same lag sums with one FP16 product (samples scaled by 1/norm, then
+ * rounded to FP16; FP32 accumulation): a third of the tensor-core work of the
+ * three-product form, coefficient errors up to ~1e-3 (typically ~1e-4).
+ * Same limits on shift and event_length.  Also a serving form. */
+#define SEISMIC_FORM_LAGGEMM_FP16 4
 
 #define SEISMIC_ERR_DEVICE_TIMEOUT 7 /* a kernel's bounded wait ran out; results invalid */
 
@@ -126,8 +131,9 @@ int seismic_check_device_error(void);
  *   outputs:  device arrays of n_events*(n_events+1)/2 entries (packed triangle);
  *   d_max_hist/d_min_hist: device int[n_classes_hist], accumulated into, or
  *             NULL with n_classes_hist == 0;
- *   workspace: device buffer of seismic_xcorr_workspace_bytes() or NULL (the
- *             library then uses its own cached allocation);
+ *   workspace: device buffer of seismic_xcorr_workspace_bytes(), 256-byte
+ *             aligned (as cudaMalloc returns), or NULL (the library then uses
+ *             its own cached allocation);
  *   stream:   a cudaStream_t (NULL = legacy default stream).
  * Asynchronous with respect to the host.  Returns a SEISMIC_* status. */
 int seismic_xcorr_device(const float *d_events, long long n_events, int n_channels, int event_length,

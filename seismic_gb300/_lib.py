@@ -19,7 +19,7 @@ c_int_p = ctypes.POINTER(ctypes.c_int)
 c_ll = ctypes.c_longlong
 
 SEISMIC_OK = 0
-FORMS = {"fp32": 0, "fp16": 1, "laggemm": 2, "bf16": 3}
+FORMS = {"fp32": 0, "fp16": 1, "laggemm": 2, "bf16": 3, "laggemm16": 4}
 
 _lib = None
 

@@ -120,6 +120,10 @@ static size_t spectra_bytes(long long rows, int P, int stype = 0) {
 }
 static size_t norms_bytes(long long rows) { return norms_buffer_bytes(rows); }
 
+static bool is_lag_form(int form) {
+  return form == SEISMIC_FORM_LAGGEMM_BF16X3 || form == SEISMIC_FORM_LAGGEMM_FP16;
+}
+
 static int validate(long long n_events, int n_channels, int event_length, int padded, int shift,
                     int n_hist, int form) {
   if (n_events < 1) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_events must be >= 1 (got %lld)", n_events);
@@ -131,13 +135,13 @@ static int validate(long long n_events, int n_channels, int event_length, int pa
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "event_length %d exceeds paddedSize %d", event_length, padded);
   if (shift < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "shift must be >= 0");
   if (n_hist < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_classes_hist must be >= 0");
-  if (form != SEISMIC_FORM_FP32 && form != SEISMIC_FORM_LAGGEMM_BF16X3 && form != SEISMIC_FORM_FP16_SPECTRA &&
+  if (form != SEISMIC_FORM_FP32 && !is_lag_form(form) && form != SEISMIC_FORM_FP16_SPECTRA &&
       form != SEISMIC_FORM_BF16_SPECTRA)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "unknown form %d", form);
-  if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
+  if (is_lag_form(form)) {
     if (shift < 1 || 2 * shift > 512)
       return set_status(SEISMIC_ERR_UNSUPPORTED_SIZE, "lag-GEMM form needs 1 <= shift <= 256 (got %d)", shift);
-    if (!lag_plan(n_events, n_channels, event_length, shift, n_hist).ok)
+    if (!lag_plan(n_events, n_channels, event_length, shift, n_hist, lag_planes(form)).ok)
       return set_status(SEISMIC_ERR_UNSUPPORTED_SIZE,
                         "lag-GEMM form: event_length %d with shift %d does not fit in shared memory", event_length,
                         shift);
@@ -249,10 +253,10 @@ int check_xcorr_args(long long n_events, int n_channels, int event_length, int p
 static int run_xcorr(const DeviceState &st, const float *d_events, long long n, int C, int L, long long ev_stride,
                      long long ch_stride, int P, int shift, float thr, int n_hist, float *vp, int *lp, float *vn,
                      int *ln, int *hmax, int *hmin, void *ws, cudaStream_t stream, int form = SEISMIC_FORM_FP32) {
-  if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
+  if (is_lag_form(form)) {
     int launched = 0;
     cudaError_t e = launch_lag_gemm(d_events, n, C, L, ev_stride, ch_stride, shift, thr, n_hist, vp, lp, vn, ln,
-                                    hmax, hmin, ws, st.error_flag, st.sm_count, stream, &launched);
+                                    hmax, hmin, ws, st.error_flag, st.sm_count, stream, &launched, form);
     g_launches.fetch_add(launched);
     SEISMIC_TRY(e, "lag-GEMM launch");
     return SEISMIC_OK;
@@ -305,9 +309,9 @@ int seismic_resolve_padded_size(int event_length, int shift) {
 size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int event_length, int shift,
                                      int padded_size, int form) {
   if (n_events < 1 || n_channels < 1 || event_length < 1) return 0;
-  if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
-    if (!lag_plan(n_events, n_channels, event_length, shift, 0).ok) return 0;
-    return lag_workspace_bytes(n_events, n_channels, event_length);
+  if (is_lag_form(form)) {
+    if (!lag_plan(n_events, n_channels, event_length, shift, 0, lag_planes(form)).ok) return 0;
+    return lag_workspace_bytes(n_events, n_channels, event_length, lag_planes(form));
   }
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
   if (!supported_padded_size(padded_size)) return 0;
@@ -352,6 +356,8 @@ int seismic_xcorr_device(const float *d_events, long long n_events, int n_channe
   if (workspace) {
     if (workspace_bytes < need)
       return set_status(SEISMIC_ERR_WORKSPACE_TOO_SMALL, "workspace %zu < %zu bytes", workspace_bytes, need);
+    if (reinterpret_cast<uintptr_t>(workspace) & 255u)  // TMA sources and 16-byte loads inside it
+      return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "workspace must be 256-byte aligned");
   } else {
     std::lock_guard<std::mutex> lock(g_mutex);
     if ((s = grow(&st->ws, &st->ws_bytes, need, "workspace allocation"))) return s;
@@ -494,13 +500,13 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
     SEISMIC_TRY(cudaMemcpyAsync(h.data(), d_hist, h.size() * sizeof(int), cudaMemcpyDeviceToHost, stream),
                 "hist D2H");
   SEISMIC_TRY(cudaStreamSynchronize(stream), "host call sync");
-  if (form == SEISMIC_FORM_LAGGEMM_BF16X3) {
+  {  // every form's kernels raise this flag when a bounded wait runs out
     int flag = 0;
     SEISMIC_TRY(cudaMemcpy(&flag, st->error_flag, sizeof(int), cudaMemcpyDeviceToHost), "error flag read");
     if (flag) {
       const int zero = 0;
       cudaMemcpy(st->error_flag, &zero, sizeof(int), cudaMemcpyHostToDevice);
-      return set_status(SEISMIC_ERR_DEVICE_TIMEOUT, "lag-GEMM kernel gave up a bounded wait; results invalid");
+      return set_status(SEISMIC_ERR_DEVICE_TIMEOUT, "a kernel gave up a bounded wait; results invalid");
     }
   }
   for (int k = 0; k < n_classes_hist; ++k) {

@@ -157,12 +157,23 @@ struct LagPlan {
   bool ok;
   int lp, nt, wt, wpad, jp, nbuf, nm, strip_bytes, xs_len, jc, stages, smem;
 };
-LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int n_hist);
-size_t lag_workspace_bytes(long long n_events, int n_channels, int length);
+// Lag forms: SEISMIC_FORM_LAGGEMM_BF16X3 (BF16 hi + lo planes, three
+// products) and SEISMIC_FORM_LAGGEMM_FP16 (one FP16 plane, one product).
+int lag_planes(int form);
+LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int n_hist, int nhl = 2);
+size_t lag_workspace_bytes(long long n_events, int n_channels, int length, int nhl = 2);
+// Prep (planes + FP64 norms) of n events into a workspace of lag_workspace_bytes.
+cudaError_t lag_prepare(const float *events, long long n, int C, int length, long long ev_stride,
+                        long long ch_stride, int form, void *ws, cudaStream_t s);
 cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length, long long ev_stride,
                             long long ch_stride, int shift, float threshold, int n_hist, float *vp, int *lp,
                             float *vn, int *ln, int *hmax, int *hmin, void *ws, int *error_flag, int sm_count,
-                            cudaStream_t s, int *launches);
+                            cudaStream_t s, int *launches, int form);
+// Rectangle: queries (prepared in q_ws) x catalog events col_begin ..
+// col_begin + n_cols - 1 (prepared in cat_ws); outputs [n_query][n_cols].
+cudaError_t launch_lag_rect(const void *cat_ws, long long n_cat, const void *q_ws, long long n_query, int C,
+                            int length, int shift, long long col_begin, long long n_cols, float threshold, int form,
+                            float *vp, int *lp, float *vn, int *ln, int *error_flag, int sm_count, cudaStream_t s);
 // Device address of the kernels' error flag (set when a bounded wait runs out).
 int *device_error_flag();
 

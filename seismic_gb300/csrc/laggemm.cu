@@ -39,10 +39,13 @@
 // for windows short enough that the direct lag sum is cheaper on tensor cores.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <climits>
 #include <cstdio>
+#include <cstdlib>
 
+#include "../../include/seismic_gb300.h"
 #include "kernels.cuh"
 #include "tcgen05.cuh"
 #include "tma_host.cuh"
@@ -57,11 +60,14 @@ constexpr int kLagThreads = 320; // 10 warps
 constexpr int kLagHistMax = 1024;
 
 // ------------------------------------------------------------------ prep
-// One warp per (event, channel) row: FP64 norm, then hi/lo BF16 split of the
-// (optionally 1/norm-scaled) samples into channel-major [C][N][Lp] arrays.
+// One warp per (event, channel) row: FP64 norm, then the hi/lo split of the
+// (optionally 1/norm-scaled) samples into channel-major [C][N][Lp] arrays of
+// 16-bit values: BF16 hi and lo (the three-product form), or FP16 hi only
+// (the one-product form; xlo null).
+template <bool F16>
 __global__ void lag_prep_kernel(const float *__restrict__ ev, long long n, int C, int L, long long ev_stride,
-                                long long ch_stride, int lp, int prescale, __nv_bfloat16 *__restrict__ xhi,
-                                __nv_bfloat16 *__restrict__ xlo, double *__restrict__ norms) {
+                                long long ch_stride, int lp, int prescale, unsigned short *__restrict__ xhi,
+                                unsigned short *__restrict__ xlo, double *__restrict__ norms) {
   const long long row = (long long)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
   if (row >= n * C) return;
@@ -77,13 +83,17 @@ __global__ void lag_prep_kernel(const float *__restrict__ ev, long long n, int C
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   const double nrm = sqrt(s);
   const float scale = prescale ? (nrm > 0.0 ? (float)(1.0 / nrm) : 0.f) : 1.f;
-  __nv_bfloat16 *dh = xhi + ((long long)c * n + e) * lp;
-  __nv_bfloat16 *dl = xlo + ((long long)c * n + e) * lp;
+  unsigned short *dh = xhi + ((long long)c * n + e) * lp;
+  unsigned short *dl = xlo ? xlo + ((long long)c * n + e) * lp : nullptr;
   for (int k = lane; k < lp; k += 32) {
     const float v = k < L ? src[k] * scale : 0.f;
-    const __nv_bfloat16 h = __float2bfloat16_rn(v);
-    dh[k] = h;
-    dl[k] = __float2bfloat16_rn(v - __bfloat162float(h));
+    if constexpr (F16) {
+      dh[k] = __half_as_ushort(__float2half_rn(v));
+    } else {
+      const __nv_bfloat16 h = __float2bfloat16_rn(v);
+      dh[k] = __bfloat16_as_ushort(h);
+      dl[k] = __bfloat16_as_ushort(__float2bfloat16_rn(v - __bfloat162float(h)));
+    }
   }
   if (lane == 0) {
     norms[row] = nrm;
@@ -93,9 +103,17 @@ __global__ void lag_prep_kernel(const float *__restrict__ ev, long long n, int C
 
 // ------------------------------------------------------------------ main
 struct LagArgs {
-  const __nv_bfloat16 *xhi, *xlo;  // [C][N][Lp]
-  const double *norms;             // [N*C], event-major
+  const unsigned short *xhi, *xlo;  // A side [C][N][Lp] 16-bit (xlo unused with one product)
+  const double *norms;              // [N*C], event-major
   long long n;
+  // Rectangle mode (rect != 0): A = catalog events col_begin .. col_begin +
+  // n_cols - 1 of the xhi/xlo arrays (n = catalog size), strips from the
+  // query arrays qhi/qlo [C][n_query][Lp]; pair (query q, catalog e) at
+  // outputs[q * n_cols + e - col_begin].  Triangle mode: strips from xhi/xlo.
+  int rect;
+  const unsigned short *qhi, *qlo;
+  const double *q_norms;
+  long long n_query, col_begin, n_cols;
   int C, L, lp;
   int shift;      // lags d = 1-shift .. shift
   int wpad;       // 2*shift rounded up to a multiple of 16*nt
@@ -118,6 +136,9 @@ struct LagArgs {
   int *max_hist, *min_hist;
   int *error_flag;
   int off_a, off_hank, off_xs, off_hist, off_bars, off_misc;  // shared-memory layout (host computed)
+  // 16-bit planes per operand: 2 (BF16 hi, lo; products hi*hi + hi*lo +
+  // lo*hi) or 1 (FP16 hi; hi*hi); the kernel is instantiated per value
+  int nhl;
 };
 
 struct LagSmem {  // offsets into dynamic shared memory (base 1024-aligned)
@@ -128,11 +149,11 @@ static LagSmem lag_smem_layout(const LagArgs &a) {
   LagSmem s;
   int off = 0;
   s.a = off;
-  off += a.stages * 2 * kLagM * kLagKC * 2;  // hi + lo tiles per stage
+  off += a.stages * a.nhl * kLagM * kLagKC * 2;  // hi (+ lo) tiles per stage
   s.hank = off;
-  off += 2 * a.jp * 2 * a.strip_bytes;  // two buffers of jp (hi, lo) strips
+  off += 2 * a.jp * a.nhl * a.strip_bytes;  // two buffers of jp (hi [, lo]) strips
   s.xs = off;
-  off += a.jp * 2 * ((a.xs_len * 2 + 15) / 16 * 16);
+  off += a.jp * a.nhl * ((a.xs_len * 2 + 15) / 16 * 16);
   s.hist = off;
   off += (a.n_hist > 0 && a.n_hist <= kLagHistMax) ? 2 * a.n_hist * 4 : 0;
   off = (off + 7) / 8 * 8;
@@ -161,12 +182,38 @@ __device__ __forceinline__ int hist_bin_lag(float v, float delta, int n_hist) {
   return b > n_hist - 1 ? n_hist - 1 : (b < 0 ? 0 : b);
 }
 
+// Column n of a pass is lag shift - n (triangle: n increasing = lag
+// decreasing, so among equal values the largest n is the first occurrence,
+// the smallest lag) or lag n - (shift - 1) (rectangle: the smallest n).
+// One scan chain over 16 columns n0 .. n0 + 15 (CHECK: only n < nvalid).
+template <bool RECT, bool CHECK>
+__device__ __forceinline__ void lag_scan16(const uint32_t (&r)[16], int n0, int nvalid, float &best, int &bn,
+                                           float &worst, int &wn) {
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const int n = n0 + k;
+    const float v = __uint_as_float(r[k]);
+    if (!CHECK || n < nvalid) {
+      if (RECT ? v > best : v >= best) { best = v; bn = n; }
+      if (RECT ? v < worst : v <= worst) { worst = v; wn = n; }
+    }
+  }
+}
+// Merge of two chains: does (v, n) win over (w, m)?  Larger (max) or
+// smaller (min) value; on equal values the first occurrence.
+template <bool RECT>
+__device__ __forceinline__ bool lag_better(float v, int n, float w, int m, bool max) {
+  if (max ? v > w : v < w) return true;
+  return v == w && (RECT ? n < m : n > m);
+}
+
 // Items: row-block b (events [128b, 128b+128)) x chunk q of j's starting at
 // 128b, each chunk `jc` events.  Advance (b, q) by `step` items.
+// Rectangle mode: every block has the same n_query j's (pass n_rect = n_query).
 __device__ __forceinline__ void advance_item(long long &b, long long &q, long long step, long long n, int jc,
-                                             long long nblk) {
+                                             long long nblk, long long n_rect = 0) {
   while (step > 0 && b < nblk) {
-    const long long rows_j = n - b * kLagM;
+    const long long rows_j = n_rect > 0 ? n_rect : n - b * kLagM;
     const long long chunks = (rows_j + jc - 1) / jc;
     const long long left = chunks - q;
     if (step < left) {
@@ -179,9 +226,13 @@ __device__ __forceinline__ void advance_item(long long &b, long long &q, long lo
   }
 }
 
+// NHL: 16-bit planes per operand (2: BF16 hi + lo, three products; 1: FP16
+// hi, one product).  RECT: query x catalog rectangle instead of the triangle.
+template <int NHL, bool RECT>
 __global__ void __launch_bounds__(kLagThreads, 1)
     lag_gemm_kernel(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
                     LagArgs a) {
+  constexpr int nhl = NHL;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base =
       reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -226,15 +277,20 @@ __global__ void __launch_bounds__(kLagThreads, 1)
   const uint32_t tmem = *tmem_slot;
 
   const long long N = a.n;
-  const long long nblk = (N + kLagM - 1) / kLagM;
+  // A-side events walked in blocks of 128: the triangle's rows, or the
+  // catalog columns col_begin .. col_begin + n_cols - 1 of a rectangle
+  const long long a_row0 = RECT ? a.col_begin : 0;
+  const long long nblk = ((RECT ? a.n_cols : N) + kLagM - 1) / kLagM;
+  const long long n_rect = RECT ? a.n_query : 0;
+  const long long n_j = RECT ? a.n_query : N;  // j's: triangle events or queries
   const int kchunks = a.lp / kLagKC;
   const int C = a.C;
-  const uint32_t tile_bytes = kLagM * kLagKC * 2;
-  const uint32_t idesc = tc::idesc_bf16_f32(kLagM, a.wt);
+  constexpr uint32_t tile_bytes = kLagM * kLagKC * 2;
+  const uint32_t idesc = tc::idesc_f16_f32(kLagM, a.wt, NHL == 1);
   const uint32_t buf_cols = (uint32_t)(a.jp * a.wpad);  // TMEM columns of one pass
 
   long long b = 0, q = 0;
-  advance_item(b, q, blockIdx.x, N, a.jc, nblk);
+  advance_item(b, q, blockIdx.x, N, a.jc, nblk, n_rect);
 
   if (warp == 4) {
     // ================================================= TMA producer (A tiles)
@@ -243,18 +299,18 @@ __global__ void __launch_bounds__(kLagThreads, 1)
       uint32_t phase = 0;
       long long it = 0;
       uint32_t issued_mask = 0, last_parity = 0;  // per stage: any load issued / parity of the latest
-      for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk)) {
-        const long long j_begin = bb * kLagM + qq * a.jc;
-        const long long j_end = min(j_begin + a.jc, N);
+      for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
+        const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
+        const long long j_end = min(j_begin + a.jc, n_j);
         for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp) {
           for (int c = 0; c < C && !*abort_flag; ++c) {
             for (int kc = 0; kc < kchunks; ++kc, ++it) {
               if (it >= a.stages && !lag_wait(&a_empty[stage], phase ^ 1, abort_flag, a.error_flag)) break;
-              unsigned char *dst = base + L.a + stage * 2 * tile_bytes;
-              tc::mbar_arrive_expect_tx(&a_full[stage], 2 * tile_bytes);
-              const int row = (int)(c * N + bb * kLagM);
+              unsigned char *dst = base + L.a + stage * nhl * tile_bytes;
+              tc::mbar_arrive_expect_tx(&a_full[stage], nhl * tile_bytes);
+              const int row = (int)(c * N + a_row0 + bb * kLagM);
               tc::tma_load_2d(dst, &tm_hi, kc * kLagKC, row, &a_full[stage]);
-              tc::tma_load_2d(dst + tile_bytes, &tm_lo, kc * kLagKC, row, &a_full[stage]);
+              if (nhl > 1) tc::tma_load_2d(dst + tile_bytes, &tm_lo, kc * kLagKC, row, &a_full[stage]);
               issued_mask |= 1u << stage;
               last_parity = (last_parity & ~(1u << stage)) | (phase << stage);
               if (++stage == a.stages) {
@@ -271,13 +327,22 @@ __global__ void __launch_bounds__(kLagThreads, 1)
     }
   } else if (warp == 5) {
     // ================================================= MMA issuer
+    // One thread issues every MMA, so the loop body is kept to a few adds:
+    // descriptors are built once and advanced by their start-address field
+    // (16-byte units; shared addresses stay below 2^18 bytes, so the field
+    // never carries), and the (j, N-tile) pairs of a pass are a fixed table.
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
       long long unit = 0, pass = 0;  // (pass, channel) strip units; passes
-      for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk)) {
-        const long long j_begin = bb * kLagM + qq * a.jc;
-        const long long j_end = min(j_begin + a.jc, N);
+      const uint64_t da0 = tc::smem_desc(smem_u32(base + L.a), 16, 1024, 2);
+      const uint64_t db0 = tc::smem_desc(smem_u32(base + L.hank), 128, 128, 0);
+      constexpr uint32_t tile_u = tile_bytes >> 4;   // A tile, descriptor units
+      const uint32_t strip_u = (uint32_t)a.strip_bytes >> 4;
+      const int nnt = a.nt;
+      for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
+        const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
+        const long long j_end = min(j_begin + a.jc, n_j);
         for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp, ++pass) {
           const int njp = (int)min((long long)a.jp, j_end - j0);
           const int tb = (int)(pass % a.nbuf);
@@ -285,32 +350,39 @@ __global__ void __launch_bounds__(kLagThreads, 1)
           if (tuse > 0 && !lag_wait(&tmem_empty[tb], (uint32_t)((tuse - 1) & 1), abort_flag, a.error_flag)) break;
           tc::fence_after_sync();
           const uint32_t tbase = tmem + (uint32_t)tb * buf_cols;
+          // (j p, N-tile nt) pairs: TMEM column of the accumulator and the
+          // strip offset of the tile's first core matrix (descriptor units)
+          const int ncombo = njp * nnt;
+          uint32_t dcol[4], boff[4];
+#pragma unroll
+          for (int cb = 0; cb < 4; ++cb) {
+            const int p = nnt == 1 ? cb : cb >> 1, nt = nnt == 1 ? 0 : cb & 1;
+            dcol[cb] = tbase + (uint32_t)(p * a.wpad + nt * a.wt);
+            boff[cb] = (uint32_t)(p * nhl) * strip_u + (uint32_t)(nt * (a.wt / 8) * 8);
+          }
           for (int c = 0; c < C && !*abort_flag; ++c, ++unit) {
             const int hb = (int)(unit & 1);
             if (!lag_wait(&hank_full[hb], (uint32_t)((unit >> 1) & 1), abort_flag, a.error_flag)) break;
             tc::fence_after_sync();
+            const uint64_t dbu = db0 + (uint64_t)((uint32_t)(hb * a.jp * nhl) * strip_u);
             for (int kc = 0; kc < kchunks; ++kc) {
               if (!lag_wait(&a_full[stage], phase, abort_flag, a.error_flag)) break;
               tc::fence_after_sync();
-              const uint32_t a_hi = smem_u32(base + L.a + stage * 2 * tile_bytes);
-              const uint32_t a_lo = a_hi + tile_bytes;
+              const uint64_t das = da0 + (uint64_t)((uint32_t)(stage * nhl) * tile_u);
 #pragma unroll
               for (int ks = 0; ks < kLagKC / 16; ++ks) {
-                const uint64_t dah = tc::smem_desc(a_hi + 32 * ks, 16, 1024, 2);
-                const uint64_t dal = tc::smem_desc(a_lo + 32 * ks, 16, 1024, 2);
-                const int h0 = kc * (kLagKC / 8) + 2 * ks;  // k core-matrix index
-                for (int p = 0; p < njp; ++p) {
-                  const uint32_t s_hi = smem_u32(base + L.hank + ((hb * a.jp + p) * 2 + 0) * a.strip_bytes);
-                  const uint32_t s_lo = s_hi + a.strip_bytes;
-                  for (int nt = 0; nt < a.nt; ++nt) {
-                    const uint32_t coff = (uint32_t)((nt * (a.wt / 8) + h0) * 128);
-                    const uint64_t dbh = tc::smem_desc(s_hi + coff, 128, 128, 0);
-                    const uint64_t dbl = tc::smem_desc(s_lo + coff, 128, 128, 0);
-                    const uint32_t d = tbase + (uint32_t)(p * a.wpad + nt * a.wt);
-                    const uint32_t acc0 = (c > 0 || kc > 0 || ks > 0) ? 1u : 0u;
-                    tc::mma_bf16(d, dah, dbh, idesc, acc0);
-                    tc::mma_bf16(d, dah, dbl, idesc, 1u);
-                    tc::mma_bf16(d, dal, dbh, idesc, 1u);
+                const uint64_t dah = das + (uint64_t)(2 * ks);  // 32 bytes of K per step
+                const uint64_t dbk = dbu + (uint64_t)((kc * (kLagKC / 8) + 2 * ks) * 8);  // k core matrix
+                const uint32_t acc0 = (c | kc | ks) != 0 ? 1u : 0u;
+#pragma unroll
+                for (int cb = 0; cb < 4; ++cb) {
+                  if (cb < ncombo) {
+                    const uint64_t dbh = dbk + boff[cb];
+                    tc::mma_bf16(dcol[cb], dah, dbh, idesc, acc0);
+                    if constexpr (NHL == 2) {  // hi*lo + lo*hi
+                      tc::mma_bf16(dcol[cb], dah, dbh + strip_u, idesc, 1u);
+                      tc::mma_bf16(dcol[cb], dah + tile_u, dbh, idesc, 1u);
+                    }
                   }
                 }
               }
@@ -332,10 +404,21 @@ __global__ void __launch_bounds__(kLagThreads, 1)
   } else if (warp < 4) {
     // ================================================= Hankel strip builders (warps 0-3)
     const int e_lane = tid;  // 0..127
+    const int xs_stride = (a.xs_len * 2 + 15) / 16 * 16;
+    // xs[u] = x[u - off]: off = shift, or shift - 1 in the rectangle, whose
+    // pairs are (j, i) (the lag of pair (query, catalog event) is the negated
+    // lag of the GEMM).  The planes hold zeros from L to lp, so each pass
+    // copies the lp samples of a row to xs[off ..]; the rest of xs stays zero
+    // from here on.
+    const int off = RECT ? a.shift - 1 : a.shift;
+    for (int w = e_lane; w < a.jp * nhl * xs_stride / 4; w += kLagM)
+      reinterpret_cast<uint32_t *>(base + L.xs)[w] = 0u;
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    const int n8 = a.lp / 8;  // 16-byte chunks per row
     long long unit = 0;
-    for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk)) {
-      const long long j_begin = bb * kLagM + qq * a.jc;
-      const long long j_end = min(j_begin + a.jc, N);
+    for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
+      const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
+      const long long j_end = min(j_begin + a.jc, n_j);
       for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp) {
         const int njp = (int)min((long long)a.jp, j_end - j0);
         for (int c = 0; c < C && !*abort_flag; ++c, ++unit) {
@@ -343,38 +426,66 @@ __global__ void __launch_bounds__(kLagThreads, 1)
           // wait until the MMAs of the unit two back (same buffer) no longer read it
           if (unit >= 2 && !lag_wait(&hank_empty[hb], (uint32_t)(((unit >> 1) - 1) & 1), abort_flag, a.error_flag))
             break;
-          const int xs_stride = (a.xs_len * 2 + 15) / 16 * 16;
-          for (int p = 0; p < njp; ++p) {
-            const long long j = j0 + p;
-            const __nv_bfloat16 *srcs[2] = {a.xhi + ((long long)c * N + j) * a.lp,
-                                            a.xlo + ((long long)c * N + j) * a.lp};
+          // rows of the j side (triangle events, or the rectangle's queries):
+          // chunks f = ((p * nhl + hl) * n8 + ch), four per thread in flight
+          const long long row0 = (long long)c * n_j + j0;
+          const int n_f = njp * nhl * n8;
+          for (int f0 = e_lane; f0 < n_f; f0 += 4 * kLagM) {
+            uint4 v[4];
 #pragma unroll
-            for (int hl = 0; hl < 2; ++hl) {
-              unsigned short *xs = reinterpret_cast<unsigned short *>(base + L.xs + (p * 2 + hl) * xs_stride);
-              const unsigned short *src = reinterpret_cast<const unsigned short *>(srcs[hl]);
-              // xs[u] = x[u - shift] (zero outside [0, L))
-              for (int u = e_lane; u < a.xs_len; u += kLagM) {
-                const int k = u - a.shift;
-                xs[u] = (k >= 0 && k < a.L) ? src[k] : (unsigned short)0;
+            for (int t = 0; t < 4; ++t) {
+              const int f = f0 + t * kLagM;
+              if (f < n_f) {
+                const int ph = f / n8, ch = f - ph * n8;
+                const int p = ph / nhl, hl = ph - p * nhl;
+                const unsigned short *plane = hl == 0 ? (RECT ? a.qhi : a.xhi) : (RECT ? a.qlo : a.xlo);
+                v[t] = __ldg(reinterpret_cast<const uint4 *>(plane + (row0 + p) * a.lp) + ch);
+              }
+            }
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const int f = f0 + t * kLagM;
+              if (f < n_f) {
+                const int ph = f / n8, ch = f - ph * n8;
+                unsigned short *xs = reinterpret_cast<unsigned short *>(base + L.xs + ph * xs_stride) + off + 8 * ch;
+                if ((off & 7) == 0) {
+                  *reinterpret_cast<uint4 *>(xs) = v[t];
+                } else if ((off & 1) == 0) {
+                  uint32_t *x2 = reinterpret_cast<uint32_t *>(xs);
+                  x2[0] = v[t].x;
+                  x2[1] = v[t].y;
+                  x2[2] = v[t].z;
+                  x2[3] = v[t].w;
+                } else {
+                  const uint32_t wv[4] = {v[t].x, v[t].y, v[t].z, v[t].w};
+#pragma unroll
+                  for (int k = 0; k < 4; ++k) {
+                    xs[2 * k] = (unsigned short)(wv[k] & 0xFFFFu);
+                    xs[2 * k + 1] = (unsigned short)(wv[k] >> 16);
+                  }
+                }
               }
             }
           }
           asm volatile("bar.sync 1, 128;" ::: "memory");
           for (int p = 0; p < njp; ++p) {
 #pragma unroll
-            for (int hl = 0; hl < 2; ++hl) {
-              const unsigned short *xs =
-                  reinterpret_cast<const unsigned short *>(base + L.xs + (p * 2 + hl) * xs_stride);
+            for (int hl = 0; hl < nhl; ++hl) {
+              const uint32_t *xw = reinterpret_cast<const uint32_t *>(base + L.xs + (p * nhl + hl) * xs_stride);
               uint4 *strip =
-                  reinterpret_cast<uint4 *>(base + L.hank + ((hb * a.jp + p) * 2 + hl) * a.strip_bytes);
-              // core matrix m, row r = xs[8m + r .. 8m + r + 7]
-              for (int rowi = e_lane; rowi < a.nm * 8; rowi += kLagM) {
-                const int o = rowi;  // 8m + r
+                  reinterpret_cast<uint4 *>(base + L.hank + ((hb * a.jp + p) * nhl + hl) * a.strip_bytes);
+              // core matrix m, row r = xs[o .. o + 7], o = 8m + r: five 32-bit
+              // words from xs[o & ~1], shifted by one sample when o is odd
+              for (int o = e_lane; o < a.nm * 8; o += kLagM) {
+                const uint32_t *src = xw + (o >> 1);
+                const uint32_t sh = 16u * (uint32_t)(o & 1);
+                uint32_t wd[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) wd[k] = src[k];
                 uint32_t w[4];
 #pragma unroll
-                for (int qd = 0; qd < 4; ++qd)
-                  w[qd] = (uint32_t)xs[o + 2 * qd] | ((uint32_t)xs[o + 2 * qd + 1] << 16);
-                strip[rowi] = make_uint4(w[0], w[1], w[2], w[3]);
+                for (int k = 0; k < 4; ++k) w[k] = __funnelshift_r(wd[k], wd[k + 1], sh);
+                strip[o] = make_uint4(w[0], w[1], w[2], w[3]);
               }
             }
           }
@@ -390,56 +501,80 @@ __global__ void __launch_bounds__(kLagThreads, 1)
     const int e_lane = 32 * quarter + lane;       // event within the block
     const uint32_t lane_addr = (uint32_t)(32 * quarter) << 16;
     long long pass = 0;
-    for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk)) {
-      const long long j_begin = bb * kLagM + qq * a.jc;
-      const long long j_end = min(j_begin + a.jc, N);
+    for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
+      const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
+      const long long j_end = min(j_begin + a.jc, n_j);
       for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp, ++pass) {
         const int njp = (int)min((long long)a.jp, j_end - j0);
         const int tb = (int)(pass % a.nbuf);
         if (!lag_wait(&tmem_full[tb], (uint32_t)((pass / a.nbuf) & 1), abort_flag, a.error_flag)) break;
         tc::fence_after_sync();
-        const long long i = bb * kLagM + e_lane;
-        for (int p = 0; p < njp; ++p) {
-          const long long j = j0 + p;
-          float best = 0.f, worst = 0.f;
-          int bn = 0, wn = 0;
-          const uint32_t col0 = (uint32_t)tb * buf_cols + (uint32_t)(p * a.wpad);
-          for (int c0 = 0; c0 < a.wpad; c0 += 64) {
-            // up to four 16-column loads in flight, one wait
-            uint32_t r[4][16];
-            const int nl = min(4, (a.wpad - c0) / 16);
+        const long long i = a_row0 + bb * kLagM + e_lane;  // A-side event
+        // extrema of the (up to two) j's of the pass, then the TMEM buffer
+        // goes back to the MMA before the normalisation and the stores
+        float bestp[2], worstp[2];
+        int bnp[2], wnp[2];
 #pragma unroll
-            for (int h = 0; h < 4; ++h)
-              if (h < nl) tc::tmem_ld16_issue(tmem + lane_addr + col0 + (uint32_t)(c0 + 16 * h), r[h]);
-            tc::tmem_ld_wait();
+        for (int p = 0; p < 2; ++p) {
+          if (p < njp) {
+            const uint32_t col0 = (uint32_t)tb * buf_cols + (uint32_t)(p * a.wpad);
+            // four scan chains (one per 16-column slice of each 64-column
+            // block), merged below: chains of 1/4 the length
+            float best[4] = {0.f, 0.f, 0.f, 0.f}, worst[4] = {0.f, 0.f, 0.f, 0.f};
+            int bn[4] = {0, 0, 0, 0}, wn[4] = {0, 0, 0, 0};
+            for (int c0 = 0; c0 < a.wpad; c0 += 64) {
+              // up to four 16-column loads in flight, one wait
+              uint32_t r[4][16];
+              const int nl = min(4, (a.wpad - c0) / 16);
 #pragma unroll
-            for (int h = 0; h < 4; ++h) {
-              if (h < nl) {
-                tc::tmem_regs_ready(r[h]);
+              for (int h = 0; h < 4; ++h)
+                if (h < nl) tc::tmem_ld16_issue(tmem + lane_addr + col0 + (uint32_t)(c0 + 16 * h), r[h]);
+              tc::tmem_ld_wait();
+              if (c0 + 64 <= 2 * a.shift) {  // every column of the block is a lag
 #pragma unroll
-                for (int k = 0; k < 16; ++k) {
-                  const int n = c0 + 16 * h + k;
-                  const float v = __uint_as_float(r[h][k]);
-                  if (n < 2 * a.shift) {
-                    // n increasing = lag decreasing: ">=" keeps the largest n among
-                    // equal values, i.e. the smallest lag (first occurrence)
-                    if (v >= best) { best = v; bn = n; }
-                    if (v <= worst) { worst = v; wn = n; }
+                for (int h = 0; h < 4; ++h) {
+                  tc::tmem_regs_ready(r[h]);
+                  lag_scan16<RECT, false>(r[h], c0 + 16 * h, 0, best[h], bn[h], worst[h], wn[h]);
+                }
+              } else {
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                  if (h < nl) {
+                    tc::tmem_regs_ready(r[h]);
+                    lag_scan16<RECT, true>(r[h], c0 + 16 * h, 2 * a.shift, best[h], bn[h], worst[h], wn[h]);
                   }
                 }
               }
             }
+#pragma unroll
+            for (int h = 1; h < 4; ++h) {
+              if (lag_better<RECT>(best[h], bn[h], best[0], bn[0], true)) { best[0] = best[h]; bn[0] = bn[h]; }
+              if (lag_better<RECT>(worst[h], wn[h], worst[0], wn[0], false)) { worst[0] = worst[h]; wn[0] = wn[h]; }
+            }
+            bestp[p] = best[0];
+            bnp[p] = bn[0];
+            worstp[p] = worst[0];
+            wnp[p] = wn[0];
           }
-          if (i < N && j >= i) {
+        }
+        tc::fence_before_sync();
+        tc::mbar_arrive(&tmem_empty[tb]);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+          const long long j = j0 + p;
+          if (p < njp && (RECT ? (i < a.col_begin + a.n_cols && i < N) : (i < N && j >= i))) {
+            const float best = bestp[p], worst = worstp[p];
+            const int bn = bnp[p], wn = wnp[p];
             // per-event 1/norm factors come from FP64 (prep kernel); per pair FP32
-            const float *inv = inverse_norms_of(a.norms, N * C);
+            const float *inv = inverse_norms_of(a.norms, N * C);  // A side
+            const float *inv_j = RECT ? inverse_norms_of(a.q_norms, a.n_query * C) : inv;
             float scale;
             bool live = false;
             if (a.prescaled) {
-              for (int cc = 0; cc < C; ++cc) live |= (inv[i * C + cc] > 0.f) && (inv[j * C + cc] > 0.f);
+              for (int cc = 0; cc < C; ++cc) live |= (inv[i * C + cc] > 0.f) && (inv_j[j * C + cc] > 0.f);
               scale = 1.0f / (float)C;
             } else {
-              const float ni = inv[i * C], nj = inv[j * C];
+              const float ni = inv[i * C], nj = inv_j[j * C];
               live = ni > 0.f && nj > 0.f;
               scale = ni * nj;
             }
@@ -448,8 +583,10 @@ __global__ void __launch_bounds__(kLagThreads, 1)
             if (live) {
               vp = best * scale;
               vn = worst * scale;
-              lp = best > 0.f ? a.shift - bn : 0;
-              ln = worst < 0.f ? a.shift - wn : 0;
+              const int lag0 = RECT ? 1 - a.shift : a.shift;  // lag at n = 0
+              const int dir = RECT ? 1 : -1;                  // lag step per n
+              lp = best > 0.f ? lag0 + dir * bn : 0;
+              ln = worst < 0.f ? lag0 + dir * wn : 0;
               if (a.n_hist > 0) {
                 const int hp = hist_bin_lag(vp, a.delta_hist, a.n_hist);
                 const int hn = hist_bin_lag(-vn, a.delta_hist, a.n_hist);
@@ -464,15 +601,13 @@ __global__ void __launch_bounds__(kLagThreads, 1)
               if (!(vp > a.threshold)) { vp = 0.f; lp = 0; }
               if (!(vn < -a.threshold)) { vn = 0.f; ln = 0; }
             }
-            const long long idx = i * N - i * (i - 1) / 2 + (j - i);
+            const long long idx = RECT ? j * a.n_cols + (i - a.col_begin) : i * N - i * (i - 1) / 2 + (j - i);
             a.vals_pos[idx] = vp;
             a.lags_pos[idx] = lp;
             a.vals_neg[idx] = vn;
             a.lags_neg[idx] = ln;
           }
         }
-        tc::fence_before_sync();
-        tc::mbar_arrive(&tmem_empty[tb]);
       }
     }
   }
@@ -502,6 +637,8 @@ int *device_error_flag() {
   return static_cast<int *>(p);
 }
 
+// 2-D map of a [rows][lp] plane of 16-bit values (copied bit for bit; BF16
+// or FP16 is the MMA's business).
 static bool make_map(CUtensorMap *m, const void *ptr, long long rows, int lp) {
   EncodeTiledFn fn = tensor_map_encoder();
   if (!fn) return false;
@@ -514,10 +651,18 @@ static bool make_map(CUtensorMap *m, const void *ptr, long long rows, int lp) {
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int n_hist) {
+// 16-bit planes per event row of a lag form: BF16 hi + lo (three products) or
+// FP16 hi (one product).
+int lag_planes(int form) { return form == SEISMIC_FORM_LAGGEMM_FP16 ? 1 : 2; }
+
+// Samples are scaled by 1/norm before rounding for the multichannel mean, and
+// always for FP16 (whose range, +-65504, raw amplitudes may exceed).
+static int lag_prescaled(int C, int nhl) { return C > 1 || nhl == 1 ? 1 : 0; }
+
+LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int n_hist, int nhl) {
   LagPlan pl{};
   pl.ok = false;
-  if (shift < 1 || 2 * shift > 512 || length < 1) return pl;
+  if (shift < 1 || 2 * shift > 512 || length < 1 || (nhl != 1 && nhl != 2)) return pl;
   pl.lp = (length + kLagKC - 1) / kLagKC * kLagKC;
   const int w = 2 * shift;
   pl.nt = w > 256 ? 2 : 1;
@@ -531,12 +676,20 @@ LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int 
   pl.xs_len = pl.wpad + pl.lp + 16;
   pl.jc = 32;
   LagArgs t{};
-  t.stages = 4;
+  t.nhl = nhl;
   t.jp = pl.jp;
   t.strip_bytes = pl.strip_bytes;
   t.xs_len = pl.xs_len;
   t.n_hist = n_hist;
-  for (pl.stages = 4; pl.stages >= 2; --pl.stages) {
+  // A-tile ring: as deep as shared memory allows, up to 8 stages (4, 8 and
+  // 10 stages of one plane ran at the same speed; SEISMIC_LAG_STAGES sets
+  // another cap, 2 .. 12)
+  int max_stages = 8;
+  if (const char *env = getenv("SEISMIC_LAG_STAGES")) {
+    const int v = atoi(env);
+    if (v >= 2 && v <= 12) max_stages = v;
+  }
+  for (pl.stages = max_stages; pl.stages >= 2; --pl.stages) {
     t.stages = pl.stages;
     pl.smem = lag_smem_layout(t).total;
     if (pl.smem <= 227 * 1024) break;
@@ -547,62 +700,52 @@ LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int 
   return pl;
 }
 
-size_t lag_workspace_bytes(long long n, int C, int length) {
+// Workspace of a lag form for n events: [hi planes][lo planes if nhl == 2][norms].
+static size_t lag_plane_bytes(long long n, int C, int lp) { return ((size_t)n * C * lp * 2 + 255) / 256 * 256; }
+
+size_t lag_workspace_bytes(long long n, int C, int length, int nhl) {
   const int lp = (length + kLagKC - 1) / kLagKC * kLagKC;
-  const size_t x = (size_t)n * C * lp * 2;
-  return 2 * ((x + 255) / 256 * 256) + norms_buffer_bytes(n * C) + 256;
+  return nhl * lag_plane_bytes(n, C, lp) + norms_buffer_bytes(n * C) + 256;
 }
 
-cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length, long long ev_stride,
-                            long long ch_stride, int shift, float threshold, int n_hist, float *vp, int *lp,
-                            float *vn, int *ln, int *hmax, int *hmin, void *ws, int *error_flag, int sm_count,
-                            cudaStream_t s, int *launches) {
-  const LagPlan pl = lag_plan(n, C, length, shift, n_hist);
-  if (!pl.ok) return cudaErrorInvalidValue;
-  const size_t x = (size_t)n * C * pl.lp * 2;
-  const size_t xb = (x + 255) / 256 * 256;
-  __nv_bfloat16 *xhi = reinterpret_cast<__nv_bfloat16 *>(ws);
-  __nv_bfloat16 *xlo = reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<char *>(ws) + xb);
-  double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(ws) + 2 * xb);
+cudaError_t lag_prepare(const float *events, long long n, int C, int length, long long ev_stride,
+                        long long ch_stride, int form, void *ws, cudaStream_t s) {
+  const int nhl = lag_planes(form);
+  const int lp = (length + kLagKC - 1) / kLagKC * kLagKC;
+  const size_t xb = lag_plane_bytes(n, C, lp);
+  unsigned short *xhi = reinterpret_cast<unsigned short *>(ws);
+  unsigned short *xlo = nhl > 1 ? reinterpret_cast<unsigned short *>(reinterpret_cast<char *>(ws) + xb) : nullptr;
+  double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(ws) + nhl * xb);
   const long long rows = n * C;
-  lag_prep_kernel<<<(unsigned)((rows + 7) / 8), 256, 0, s>>>(events, n, C, length, ev_stride, ch_stride, pl.lp,
-                                                             C > 1 ? 1 : 0, xhi, xlo, norms);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  ++*launches;
+  const unsigned grid = (unsigned)((rows + 7) / 8);
+  if (nhl == 1)
+    lag_prep_kernel<true><<<grid, 256, 0, s>>>(events, n, C, length, ev_stride, ch_stride, lp, lag_prescaled(C, nhl),
+                                               xhi, nullptr, norms);
+  else
+    lag_prep_kernel<false><<<grid, 256, 0, s>>>(events, n, C, length, ev_stride, ch_stride, lp,
+                                                lag_prescaled(C, nhl), xhi, xlo, norms);
+  return cudaGetLastError();
+}
 
+// Shared set-up and launch of lag_gemm_kernel once `a` holds the operands.
+static cudaError_t launch_lag_kernel(LagArgs &a, const LagPlan &pl, const unsigned short *a_hi,
+                                     const unsigned short *a_lo, long long a_rows, long long items, int sm_count,
+                                     cudaStream_t s) {
   CUtensorMap mhi, mlo;
-  if (!make_map(&mhi, xhi, rows, pl.lp) || !make_map(&mlo, xlo, rows, pl.lp)) return cudaErrorInvalidValue;
-  LagArgs a{};
-  a.xhi = xhi;
-  a.xlo = xlo;
-  a.norms = norms;
-  a.n = n;
-  a.C = C;
-  a.L = length;
+  if (!make_map(&mhi, a_hi, a_rows, pl.lp)) return cudaErrorInvalidValue;
+  if (!make_map(&mlo, a_lo ? a_lo : a_hi, a_rows, pl.lp)) return cudaErrorInvalidValue;
   a.lp = pl.lp;
-  a.shift = shift;
   a.wpad = pl.wpad;
   a.nt = pl.nt;
   a.wt = pl.wt;
   a.jp = pl.jp;
   a.nbuf = pl.nbuf;
-  a.jc = pl.jc;
   a.nm = pl.nm;
   a.strip_bytes = pl.strip_bytes;
   a.xs_len = pl.xs_len;
   a.stages = pl.stages;
-  a.prescaled = C > 1 ? 1 : 0;
-  a.threshold = threshold;
-  a.n_hist = n_hist;
-  a.delta_hist = n_hist > 0 ? (float)(1.0 / n_hist) : 0.f;
-  a.vals_pos = vp;
-  a.lags_pos = lp;
-  a.vals_neg = vn;
-  a.lags_neg = ln;
-  a.max_hist = hmax;
-  a.min_hist = hmin;
-  a.error_flag = error_flag;
+  a.prescaled = lag_prescaled(a.C, a.nhl);
+  a.delta_hist = a.n_hist > 0 ? (float)(1.0 / a.n_hist) : 0.f;
   {
     const LagSmem lay = lag_smem_layout(a);
     a.off_a = lay.a;
@@ -612,20 +755,99 @@ cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length,
     a.off_bars = lay.bars;
     a.off_misc = lay.misc;
   }
-  static int configured = 0;
-  if (configured < pl.smem) {
-    e = cudaFuncSetAttribute(lag_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  void (*kern)(const CUtensorMap, const CUtensorMap, LagArgs) =
+      a.nhl == 1 ? (a.rect ? lag_gemm_kernel<1, true> : lag_gemm_kernel<1, false>)
+                 : (a.rect ? lag_gemm_kernel<2, true> : lag_gemm_kernel<2, false>);
+  static bool configured[4] = {false, false, false, false};
+  const int kid = (a.nhl == 1 ? 0 : 2) + (a.rect ? 1 : 0);
+  if (!configured[kid]) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return e;
-    configured = 227 * 1024;
+    configured[kid] = true;
   }
+  if (items <= 0) return cudaSuccess;
+  const long long grid = items < sm_count ? items : sm_count;
+  kern<<<(unsigned)grid, kLagThreads, pl.smem, s>>>(mhi, mlo, a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length, long long ev_stride,
+                            long long ch_stride, int shift, float threshold, int n_hist, float *vp, int *lp,
+                            float *vn, int *ln, int *hmax, int *hmin, void *ws, int *error_flag, int sm_count,
+                            cudaStream_t s, int *launches, int form) {
+  const int nhl = lag_planes(form);
+  const LagPlan pl = lag_plan(n, C, length, shift, n_hist, nhl);
+  if (!pl.ok) return cudaErrorInvalidValue;
+  cudaError_t e = lag_prepare(events, n, C, length, ev_stride, ch_stride, form, ws, s);
+  if (e != cudaSuccess) return e;
+  ++*launches;
+  const size_t xb = lag_plane_bytes(n, C, pl.lp);
+  const unsigned short *xhi = reinterpret_cast<const unsigned short *>(ws);
+  const unsigned short *xlo = nhl > 1 ? reinterpret_cast<const unsigned short *>(reinterpret_cast<char *>(ws) + xb)
+                                      : nullptr;
+  LagArgs a{};
+  a.xhi = xhi;
+  a.xlo = xlo;
+  a.norms = reinterpret_cast<const double *>(reinterpret_cast<const char *>(ws) + nhl * xb);
+  a.n = n;
+  a.C = C;
+  a.L = length;
+  a.shift = shift;
+  a.nhl = nhl;
+  a.jc = pl.jc;
+  a.threshold = threshold;
+  a.n_hist = n_hist;
+  a.vals_pos = vp;
+  a.lags_pos = lp;
+  a.vals_neg = vn;
+  a.lags_neg = ln;
+  a.max_hist = hmax;
+  a.min_hist = hmin;
+  a.error_flag = error_flag;
   const long long nblk = (n + kLagM - 1) / kLagM;
   long long items = 0;
   for (long long bb = 0; bb < nblk; ++bb) items += (n - bb * kLagM + pl.jc - 1) / pl.jc;
-  const long long grid = items < sm_count ? items : sm_count;
-  lag_gemm_kernel<<<(unsigned)grid, kLagThreads, pl.smem, s>>>(mhi, mlo, a);
-  e = cudaGetLastError();
+  e = launch_lag_kernel(a, pl, xhi, xlo, n * C, items, sm_count, s);
   if (e == cudaSuccess) ++*launches;
   return e;
+}
+
+cudaError_t launch_lag_rect(const void *cat_ws, long long n_cat, const void *q_ws, long long n_query, int C,
+                            int length, int shift, long long col_begin, long long n_cols, float threshold, int form,
+                            float *vp, int *lp, float *vn, int *ln, int *error_flag, int sm_count, cudaStream_t s) {
+  const int nhl = lag_planes(form);
+  LagPlan pl = lag_plan(n_cat, C, length, shift, 0, nhl);
+  if (!pl.ok || col_begin < 0 || n_cols < 1 || col_begin + n_cols > n_cat || n_query < 1)
+    return cudaErrorInvalidValue;
+  pl.jc = 8;  // queries per item: more items than SMs for a 64-query request
+  const size_t cb = lag_plane_bytes(n_cat, C, pl.lp), qb = lag_plane_bytes(n_query, C, pl.lp);
+  const char *cw = static_cast<const char *>(cat_ws), *qw = static_cast<const char *>(q_ws);
+  LagArgs a{};
+  a.rect = 1;
+  a.xhi = reinterpret_cast<const unsigned short *>(cw);
+  a.xlo = nhl > 1 ? reinterpret_cast<const unsigned short *>(cw + cb) : nullptr;
+  a.norms = reinterpret_cast<const double *>(cw + nhl * cb);
+  a.qhi = reinterpret_cast<const unsigned short *>(qw);
+  a.qlo = nhl > 1 ? reinterpret_cast<const unsigned short *>(qw + qb) : nullptr;
+  a.q_norms = reinterpret_cast<const double *>(qw + nhl * qb);
+  a.n = n_cat;
+  a.n_query = n_query;
+  a.col_begin = col_begin;
+  a.n_cols = n_cols;
+  a.C = C;
+  a.L = length;
+  a.shift = shift;
+  a.nhl = nhl;
+  a.jc = pl.jc;
+  a.threshold = threshold;
+  a.vals_pos = vp;
+  a.lags_pos = lp;
+  a.vals_neg = vn;
+  a.lags_neg = ln;
+  a.error_flag = error_flag;
+  const long long nblk = (n_cols + kLagM - 1) / kLagM;
+  const long long items = nblk * ((n_query + pl.jc - 1) / pl.jc);
+  return launch_lag_kernel(a, pl, a.xhi, a.xlo, n_cat * C, items, sm_count, s);
 }
 
 }  // namespace seismic

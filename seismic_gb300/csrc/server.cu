@@ -143,6 +143,9 @@ struct seismic_server {
   float threshold = 0.f;
   void *cat_spectra = nullptr;
   double *cat_norms = nullptr;
+  // lag forms (SEISMIC_FORM_LAGGEMM_*): the catalog's 16-bit planes + norms
+  int lag_form = 0;
+  void *cat_lag = nullptr;
   int sm_count = 0;
   const float2 *tw = nullptr;
   int *error_flag = nullptr;  // device flag set by a bounded wait that ran out
@@ -169,11 +172,18 @@ namespace {
 
 size_t round256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// Bytes of the per-request transforms of the queries: spectra + norms, or the
+// lag form's planes + norms.
+size_t query_prep_bytes(const seismic_server *s, int nq) {
+  const size_t rows = (size_t)nq * s->C;
+  if (s->lag_form) return round256(lag_workspace_bytes(nq, s->C, s->L, lag_planes(s->lag_form)));
+  return round256(rows * (s->P / 2) * (s->stype ? 4 : 8)) + norms_buffer_bytes((long long)rows);
+}
+
 size_t request_bytes(const seismic_server *s, int nq, long long ncols) {
   const size_t rows = (size_t)nq * s->C;
   size_t b = round256(rows * s->L * sizeof(float));                             // query events
-  b += round256(rows * (s->P / 2) * (s->stype ? 4 : 8));                        // query spectra
-  b += norms_buffer_bytes((long long)rows);                                     // query norms
+  b += query_prep_bytes(s, nq);                                                 // query spectra / planes
   b += 4 * round256((size_t)nq * ncols * 4);                                    // outputs
   b += round256((size_t)nq * s->topk * 4) + round256((size_t)nq * s->topk * 8);  // top-K
   return b;
@@ -233,10 +243,9 @@ int launch_request(seismic_server *s, Request *r) {
   char *base = s->pool + r->pool_off;
   float *q_ev = reinterpret_cast<float *>(base);
   base += round256(rows * s->L * sizeof(float));
-  void *q_spec = base;
-  base += round256(rows * (s->P / 2) * (s->stype ? 4 : 8));
-  double *q_norm = reinterpret_cast<double *>(base);
-  base += norms_buffer_bytes((long long)rows);
+  void *q_spec = base;  // spectra, or the lag form's planes
+  double *q_norm = reinterpret_cast<double *>(base + round256(rows * (s->P / 2) * (s->stype ? 4 : 8)));
+  base += query_prep_bytes(s, nq);
   const size_t ob = round256((size_t)nq * r->n_cols * 4);
   float *d_vp = reinterpret_cast<float *>(base);
   int *d_lp = reinterpret_cast<int *>(base + ob);
@@ -247,6 +256,14 @@ int launch_request(seismic_server *s, Request *r) {
   long long *d_ti = reinterpret_cast<long long *>(base + round256((size_t)nq * s->topk * 4));
 
   cudaError_t e = cudaMemcpyAsync(q_ev, r->query, rows * s->L * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (s->lag_form) {  // time-domain lag sums on the tensor cores
+    if (e == cudaSuccess)
+      e = lag_prepare(q_ev, nq, s->C, s->L, (long long)s->C * s->L, s->L, s->lag_form, q_spec, st);
+    if (e == cudaSuccess)
+      e = launch_lag_rect(s->cat_lag, s->n_cat, q_spec, nq, s->C, s->L, s->shift, r->col_begin, r->n_cols,
+                          s->threshold, s->lag_form, d_vp, d_lp, d_vn, d_ln, s->error_flag, s->sm_count, st);
+    note_launches(2);
+  } else {
   SpectraArgs sa{};
   sa.events = q_ev;
   sa.n_events = nq;
@@ -288,6 +305,7 @@ int launch_request(seismic_server *s, Request *r) {
   pa.couple_begin = 0;
   pa.couple_end = pair_work_total(s->P, pa);
   if (e == cudaSuccess) e = launch_pair_work(s->P, pa, s->sm_count, 0, st);
+  }
   if (e == cudaSuccess && s->topk > 0) {
     topk_kernel<<<nq, kTopKThreads, 0, st>>>(d_vp, r->n_cols, s->topk, r->col_begin, d_tv, d_ti);
     e = cudaGetLastError();
@@ -363,10 +381,11 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   report_status(SEISMIC_OK, "");
   if (!out) return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "null output handle");
   *out = nullptr;
-  if (form != SEISMIC_FORM_FP32 && form != SEISMIC_FORM_FP16_SPECTRA)
-    return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "server forms: FP32 or FP16 spectra");
+  const bool lag = form == SEISMIC_FORM_LAGGEMM_BF16X3 || form == SEISMIC_FORM_LAGGEMM_FP16;
+  if (form != SEISMIC_FORM_FP32 && form != SEISMIC_FORM_FP16_SPECTRA && !lag)
+    return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "server forms: FP32 or FP16 spectra, or a lag-GEMM form");
   const int P = seismic_resolve_padded_size(event_length, shift);
-  int s0 = check_xcorr_args(n_catalog, n_channels, event_length, P, shift, 0, SEISMIC_FORM_FP32);
+  int s0 = check_xcorr_args(n_catalog, n_channels, event_length, P, shift, 0, lag ? form : SEISMIC_FORM_FP32);
   if (s0) return s0;
   if (!catalog) return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "null catalog");
   if (n_slots < 1 || n_slots > 64 || max_query_events < 1 || topk < 0 || topk > kTopKMax)
@@ -384,6 +403,7 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   s->shift = shift;
   s->threshold = threshold;
   s->stype = form == SEISMIC_FORM_FP16_SPECTRA ? 1 : 0;
+  s->lag_form = lag ? form : 0;
   s->prescale = (n_channels > 1 || s->stype) ? 1 : 0;
   s->topk = topk;
   s->sm_count = sm;
@@ -392,12 +412,22 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   s->max_query = max_query_events;
   const long long rows = n_catalog * n_channels;
   float *d_cat = nullptr;
-  cudaError_t e = cudaMalloc(&s->cat_spectra, (size_t)rows * (P / 2) * (s->stype ? 4 : 8));
-  if (e == cudaSuccess) e = cudaMalloc(&s->cat_norms, norms_buffer_bytes(rows));
+  cudaError_t e = cudaSuccess;
+  if (lag) {
+    e = cudaMalloc(&s->cat_lag, lag_workspace_bytes(n_catalog, n_channels, event_length, lag_planes(form)));
+  } else {
+    e = cudaMalloc(&s->cat_spectra, (size_t)rows * (P / 2) * (s->stype ? 4 : 8));
+    if (e == cudaSuccess) e = cudaMalloc(&s->cat_norms, norms_buffer_bytes(rows));
+  }
   if (e == cudaSuccess) e = cudaMalloc(&d_cat, (size_t)rows * event_length * sizeof(float));
   if (e == cudaSuccess)
     e = cudaMemcpy(d_cat, catalog, (size_t)rows * event_length * sizeof(float), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) {
+  if (e == cudaSuccess && lag) {
+    e = lag_prepare(d_cat, n_catalog, n_channels, event_length, (long long)n_channels * event_length,
+                    event_length, form, s->cat_lag, nullptr);
+    note_launches(1);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  } else if (e == cudaSuccess) {
     SpectraArgs sa{};
     sa.events = d_cat;
     sa.n_events = n_catalog;
@@ -425,6 +455,7 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   if (e != cudaSuccess) {
     cudaFree(s->cat_spectra);
     cudaFree(s->cat_norms);
+    cudaFree(s->cat_lag);
     cudaFree(s->pool);
     delete s;
     return report_cuda(e, "server set-up");
@@ -528,6 +559,7 @@ extern "C" int seismic_server_destroy(seismic_server *s) {
   for (auto &kv : s->by_ticket) delete kv.second;
   cudaFree(s->cat_spectra);
   cudaFree(s->cat_norms);
+  cudaFree(s->cat_lag);
   cudaFree(s->pool);
   delete s;
   return SEISMIC_OK;

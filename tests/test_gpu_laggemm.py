@@ -90,3 +90,37 @@ def test_laggemm_rejects_long_windows(cuda_ok):
     ev = synth.ricker_catalog(4, 1024, seed=56)
     with pytest.raises(_lib.SeismicError):
         xcorr.xcorr(ev, 300, form="laggemm")
+
+
+@pytest.mark.parametrize("n,c,length,shift", [(300, 1, 1024, 128), (140, 3, 512, 256)])
+def test_laggemm_fp16_one_product(cuda_ok, n, c, length, shift):
+    """SEISMIC_FORM_LAGGEMM_FP16: one FP16 product per lag sum.  Bar for this
+    form: coefficients within 2e-3 of FP64, lags identical where the FP64 top
+    two peaks are further apart than twice that, histogram totals exact."""
+    tol = 2e-3
+    ev = synth.family_catalog(n, c, length, n_families=8, seed=n + c)
+    res = xcorr.xcorr(ev, shift, threshold=0.0, n_classes_hist=16, form="laggemm16")
+    i, j = O.triu_pairs(n)
+    r = O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(length, shift))
+    ag = O.agreement(res.vals_pos, res.lags_pos, res.vals_neg, res.lags_neg, r, gap_tol=2 * tol)
+    assert ag.max_err_pos < tol and ag.max_err_neg < tol, ag
+    assert ag.lag_mismatch == 0, ag
+    assert int(res.max_hist.sum()) == i.size and int(res.min_hist.sum()) == i.size
+
+
+@pytest.mark.parametrize("amplitude", [3e5, 1e-6])
+def test_laggemm_fp16_amplitude_range(cuda_ok, amplitude):
+    """One-channel catalogs far outside FP16's range (max 65504, normal floor
+    6.1e-5): the FP16 planes hold samples scaled by 1/norm, so the result is
+    the same as at unit amplitude."""
+    tol = 2e-3
+    n, length, shift = 96, 512, 64
+    ev = synth.family_catalog(n, 1, length, n_families=6, seed=7).astype(np.float32)
+    ev = (ev / np.abs(ev).max() * amplitude).astype(np.float32)
+    res = xcorr.xcorr(ev, shift, threshold=0.0, n_classes_hist=16, form="laggemm16")
+    i, j = O.triu_pairs(n)
+    r = O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(length, shift))
+    assert np.all(np.isfinite(res.vals_pos)) and np.all(np.isfinite(res.vals_neg))
+    ag = O.agreement(res.vals_pos, res.lags_pos, res.vals_neg, res.lags_neg, r, gap_tol=2 * tol)
+    assert ag.max_err_pos < tol and ag.max_err_neg < tol, ag
+    assert ag.lag_mismatch == 0, ag

@@ -141,6 +141,9 @@ def test_device_api_torch_stream_and_workspace(cuda_ok):
     small = torch.empty(16, dtype=torch.uint8, device="cuda")
     with pytest.raises(_lib.SeismicError):
         xcorr.xcorr(t, 200, workspace=small)
+    big = torch.empty(ws.numel() + 256, dtype=torch.uint8, device="cuda")
+    with pytest.raises(_lib.SeismicError, match="aligned"):
+        xcorr.xcorr(t, 200, workspace=big[16:])  # enough bytes, not 256-byte aligned
 
 
 @pytest.mark.parametrize("n,length,shift", [(150, 200, 56), (70, 2048, 2048)])  # direct form (P=256), staged form

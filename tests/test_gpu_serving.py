@@ -24,7 +24,7 @@ def _fp64_block(cat, query, shift, b, e):
     return O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(cat.shape[-1], shift))
 
 
-@pytest.mark.parametrize("form,tol", [("fp32", 1e-5), ("fp16", 1e-3)])
+@pytest.mark.parametrize("form,tol", [("fp32", 1e-5), ("fp16", 1e-3), ("laggemm", 1e-4), ("laggemm16", 2e-3)])
 def test_server_results_vs_fp64(cuda_ok, form, tol):
     from seismic_gb300.serving import Server
     cat = _catalog()
@@ -46,12 +46,13 @@ def test_server_results_vs_fp64(cuda_ok, form, tol):
     srv.close()
 
 
-def test_server_same_result_alone_and_in_the_mix(cuda_ok):
+@pytest.mark.parametrize("form", ["fp16", "laggemm16"])
+def test_server_same_result_alone_and_in_the_mix(cuda_ok, form):
     """A request gives bit-identical results alone and when it is admitted
     while many other requests of different sizes are on the device."""
     from seismic_gb300.serving import Server
     cat = _catalog()
-    srv = Server(cat, shift=128, form="fp16", n_slots=4, max_query_events=32, topk=16)
+    srv = Server(cat, shift=128, form=form, n_slots=4, max_query_events=32, topk=16)
     probe = synth.family_catalog(7, 3, 512, n_families=2, seed=73)
     alone = srv.wait(srv.submit(probe, subset=(10, 590)))
     rng = np.random.default_rng(5)
