@@ -155,7 +155,7 @@ TuneEntry tune_lookup(int P, int n_channels);
 // ---- lag-GEMM form (laggemm.cu): time-domain lag sums on tcgen05 tensor cores
 struct LagPlan {
   bool ok;
-  int lp, nt, wt, wpad, jp, nbuf, nm, strip_bytes, xs_len, jc, stages, smem;
+  int lp, nt, wt, wpad, jp, nbuf, nm, strip_bytes, xs_len, jc, stages, smem, kgroup;
 };
 // Lag forms: SEISMIC_FORM_LAGGEMM_BF16X3 (BF16 hi + lo planes, three
 // products) and SEISMIC_FORM_LAGGEMM_FP16 (one FP16 plane, one product).

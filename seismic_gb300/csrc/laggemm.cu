@@ -58,6 +58,7 @@ constexpr int kLagM = 128;       // events per I-block (MMA M)
 constexpr int kLagKC = 64;       // samples per A tile (one 128-byte swizzle row)
 constexpr int kLagThreads = 320; // 10 warps
 constexpr int kLagHistMax = 1024;
+constexpr int kLagGroupMax = 4;  // K-chunks whose MMAs interleave
 
 // ------------------------------------------------------------------ prep
 // One warp per (event, channel) row: FP64 norm, then the hi/lo split of the
@@ -139,6 +140,7 @@ struct LagArgs {
   // 16-bit planes per operand: 2 (BF16 hi, lo; products hi*hi + hi*lo +
   // lo*hi) or 1 (FP16 hi; hi*hi); the kernel is instantiated per value
   int nhl;
+  int kgroup;     // K-chunks per MMA group (1 .. kLagGroupMax, at most stages / 2)
 };
 
 struct LagSmem {  // offsets into dynamic shared memory (base 1024-aligned)
@@ -205,6 +207,35 @@ template <bool RECT>
 __device__ __forceinline__ bool lag_better(float v, int n, float w, int m, bool max) {
   if (max ? v > w : v < w) return true;
   return v == w && (RECT ? n < m : n > m);
+}
+
+// The MMAs of a group of G K-chunks (A tiles at descriptors dat[t], Hankel
+// strips from dbg + t chunks): for each 16-sample K offset, the chunks' MMAs
+// back to back for each of NC (j, N-tile) accumulators.  An MMA that opens a
+// new K offset costs several times one that follows at the same offset with
+// another B operand, so this order is much faster than chunk after chunk.
+template <int NHL, int G, int NC>
+__device__ __forceinline__ void lag_mma_group(const uint32_t (&dcol)[2], const uint32_t (&boff)[2],
+                                              const uint64_t (&dat)[G], uint64_t dbg, uint32_t strip_u,
+                                              uint32_t idesc, uint32_t acc_first) {
+  constexpr uint32_t tile_u = kLagM * kLagKC * 2 / 16;
+#pragma unroll
+  for (int ks = 0; ks < kLagKC / 16; ++ks) {
+#pragma unroll
+    for (int t = 0; t < G; ++t) {
+      const uint64_t dah = dat[t] + (uint64_t)(2 * ks);  // 32 bytes of K per step
+      const uint64_t dbk = dbg + (uint64_t)((t * (kLagKC / 8) + 2 * ks) * 8);  // k core matrix
+#pragma unroll
+      for (int cb = 0; cb < NC; ++cb) {
+        const uint64_t dbh = dbk + boff[cb];
+        tc::mma_bf16(dcol[cb], dah, dbh, idesc, (ks | t) == 0 ? acc_first : 1u);
+        if constexpr (NHL == 2) {  // hi*lo + lo*hi
+          tc::mma_bf16(dcol[cb], dah, dbh + strip_u, idesc, 1u);
+          tc::mma_bf16(dcol[cb], dah + tile_u, dbh, idesc, 1u);
+        }
+      }
+    }
+  }
 }
 
 // Items: row-block b (events [128b, 128b+128)) x chunk q of j's starting at
@@ -340,6 +371,7 @@ __global__ void __launch_bounds__(kLagThreads, 1)
       constexpr uint32_t tile_u = tile_bytes >> 4;   // A tile, descriptor units
       const uint32_t strip_u = (uint32_t)a.strip_bytes >> 4;
       const int nnt = a.nt;
+      constexpr int kFastGroup = NHL == 1 ? 4 : 2;  // K-chunks of the unrolled group
       for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
         const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
         const long long j_end = min(j_begin + a.jc, n_j);
@@ -352,10 +384,10 @@ __global__ void __launch_bounds__(kLagThreads, 1)
           const uint32_t tbase = tmem + (uint32_t)tb * buf_cols;
           // (j p, N-tile nt) pairs: TMEM column of the accumulator and the
           // strip offset of the tile's first core matrix (descriptor units)
-          const int ncombo = njp * nnt;
-          uint32_t dcol[4], boff[4];
+          const int ncombo = njp * nnt;  // 1 or 2 (jp = 2 only with nt = 1)
+          uint32_t dcol[2], boff[2];
 #pragma unroll
-          for (int cb = 0; cb < 4; ++cb) {
+          for (int cb = 0; cb < 2; ++cb) {
             const int p = nnt == 1 ? cb : cb >> 1, nt = nnt == 1 ? 0 : cb & 1;
             dcol[cb] = tbase + (uint32_t)(p * a.wpad + nt * a.wt);
             boff[cb] = (uint32_t)(p * nhl) * strip_u + (uint32_t)(nt * (a.wt / 8) * 8);
@@ -365,31 +397,73 @@ __global__ void __launch_bounds__(kLagThreads, 1)
             if (!lag_wait(&hank_full[hb], (uint32_t)((unit >> 1) & 1), abort_flag, a.error_flag)) break;
             tc::fence_after_sync();
             const uint64_t dbu = db0 + (uint64_t)((uint32_t)(hb * a.jp * nhl) * strip_u);
-            for (int kc = 0; kc < kchunks; ++kc) {
-              if (!lag_wait(&a_full[stage], phase, abort_flag, a.error_flag)) break;
-              tc::fence_after_sync();
-              const uint64_t das = da0 + (uint64_t)((uint32_t)(stage * nhl) * tile_u);
-#pragma unroll
-              for (int ks = 0; ks < kLagKC / 16; ++ks) {
-                const uint64_t dah = das + (uint64_t)(2 * ks);  // 32 bytes of K per step
-                const uint64_t dbk = dbu + (uint64_t)((kc * (kLagKC / 8) + 2 * ks) * 8);  // k core matrix
-                const uint32_t acc0 = (c | kc | ks) != 0 ? 1u : 0u;
-#pragma unroll
-                for (int cb = 0; cb < 4; ++cb) {
-                  if (cb < ncombo) {
-                    const uint64_t dbh = dbk + boff[cb];
-                    tc::mma_bf16(dcol[cb], dah, dbh, idesc, acc0);
-                    if constexpr (NHL == 2) {  // hi*lo + lo*hi
-                      tc::mma_bf16(dcol[cb], dah, dbh + strip_u, idesc, 1u);
-                      tc::mma_bf16(dcol[cb], dah + tile_u, dbh, idesc, 1u);
-                    }
+            // K-chunks in groups of `kgroup` ring stages; within a group the
+            // MMAs of one K-step offset are issued back to back for every
+            // chunk (same accumulator, different operands), which keeps the
+            // tensor pipe busier than one chunk's K-steps in a row
+            for (int kc0 = 0; kc0 < kchunks && !*abort_flag; kc0 += a.kgroup) {
+              const int g = min(a.kgroup, kchunks - kc0);
+              bool ok = true;
+              {
+                int st = stage;
+                uint32_t ph = phase;
+                for (int t = 0; t < g; ++t) {
+                  if (!lag_wait(&a_full[st], ph, abort_flag, a.error_flag)) {
+                    ok = false;
+                    break;
+                  }
+                  if (++st == a.stages) {
+                    st = 0;
+                    ph ^= 1;
                   }
                 }
               }
-              tc::mma_commit(&a_empty[stage]);
-              if (++stage == a.stages) {
-                stage = 0;
-                phase ^= 1;
+              if (!ok) break;
+              tc::fence_after_sync();
+              if (g == kFastGroup && ncombo <= 2) {
+                // the common cases, fully unrolled: a few adds per MMA
+                uint64_t dat[kFastGroup];
+                int st = stage;
+#pragma unroll
+                for (int t = 0; t < kFastGroup; ++t) {
+                  dat[t] = da0 + (uint64_t)((uint32_t)(st * nhl) * tile_u);
+                  if (++st == a.stages) st = 0;
+                }
+                const uint64_t dbg = dbu + (uint64_t)(kc0 * (kLagKC / 8) * 8);
+                const uint32_t acc_first = (c | kc0) != 0 ? 1u : 0u;
+                if (ncombo == 1)
+                  lag_mma_group<NHL, kFastGroup, 1>(dcol, boff, dat, dbg, strip_u, idesc, acc_first);
+                else
+                  lag_mma_group<NHL, kFastGroup, 2>(dcol, boff, dat, dbg, strip_u, idesc, acc_first);
+              } else {  // a group cut short by the end of the row (lp / 64 not a multiple)
+#pragma unroll 1
+                for (int ks = 0; ks < kLagKC / 16; ++ks) {
+                  int st = stage;
+#pragma unroll 1
+                  for (int t = 0; t < g; ++t) {
+                    const uint64_t dah = da0 + (uint64_t)((uint32_t)(st * nhl) * tile_u + 2 * ks);
+                    const uint64_t dbk = dbu + (uint64_t)(((kc0 + t) * (kLagKC / 8) + 2 * ks) * 8);
+                    const uint32_t acc0 = (c | kc0 | ks | t) != 0 ? 1u : 0u;
+#pragma unroll 1
+                    for (int cb = 0; cb < ncombo; ++cb) {
+                      const uint64_t dbh = dbk + (cb == 0 ? boff[0] : boff[1]);
+                      const uint32_t d = cb == 0 ? dcol[0] : dcol[1];
+                      tc::mma_bf16(d, dah, dbh, idesc, acc0);
+                      if constexpr (NHL == 2) {
+                        tc::mma_bf16(d, dah, dbh + strip_u, idesc, 1u);
+                        tc::mma_bf16(d, dah + tile_u, dbh, idesc, 1u);
+                      }
+                    }
+                    if (++st == a.stages) st = 0;
+                  }
+                }
+              }
+              for (int t = 0; t < g; ++t) {
+                tc::mma_commit(&a_empty[stage]);
+                if (++stage == a.stages) {
+                  stage = 0;
+                  phase ^= 1;
+                }
               }
             }
             tc::mma_commit(&hank_empty[hb]);  // this unit's strips are no longer read
@@ -695,6 +769,14 @@ LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int 
     if (pl.smem <= 227 * 1024) break;
   }
   pl.ok = pl.smem <= 227 * 1024;
+  // MMA groups of up to four K-chunks, with at least as many stages again
+  // in the ring for the TMA to fill meanwhile (SEISMIC_LAG_KGROUP overrides)
+  pl.kgroup = pl.stages / 2 < kLagGroupMax ? pl.stages / 2 : kLagGroupMax;
+  if (const char *env = getenv("SEISMIC_LAG_KGROUP")) {
+    const int v = atoi(env);
+    if (v >= 1 && v <= kLagGroupMax && v <= pl.stages) pl.kgroup = v;
+  }
+  if (pl.kgroup < 1) pl.kgroup = 1;
   (void)n_events;
   (void)n_channels;
   return pl;
@@ -744,6 +826,7 @@ static cudaError_t launch_lag_kernel(LagArgs &a, const LagPlan &pl, const unsign
   a.strip_bytes = pl.strip_bytes;
   a.xs_len = pl.xs_len;
   a.stages = pl.stages;
+  a.kgroup = pl.kgroup;
   a.prescaled = lag_prescaled(a.C, a.nhl);
   a.delta_hist = a.n_hist > 0 ? (float)(1.0 / a.n_hist) : 0.f;
   {

@@ -4,6 +4,10 @@ seismic_server_* of include/seismic_gb300.h).
     srv = Server(catalog, shift=256, form="fp16", n_slots=4, topk=16)
     t = srv.submit(query_events, subset=(0, 50000))   # returns at once
     res = srv.wait(t)                                 # results + latency
+
+Forms: "fp32" / "fp16" (catalog spectra, any lag window), "laggemm" /
+"laggemm16" (catalog 16-bit sample planes and tensor-core lag sums, lag
+windows up to +-256; "laggemm16" is the fastest of them).
 """
 from __future__ import annotations
 

@@ -1,12 +1,15 @@
-"""GPU tests of the tensor-core lag-GEMM form (SEISMIC_FORM_LAGGEMM_BF16X3).
+"""GPU tests of the tensor-core lag-GEMM forms (SEISMIC_FORM_LAGGEMM_BF16X3
+and SEISMIC_FORM_LAGGEMM_FP16).
 
-It computes the linear correlation over lags 1-shift .. shift directly in
-the time domain (BF16 hi+lo split, three products, FP32 accumulation), so it
-is compared with the FP64 oracle and with the FP32 FFT form run at a padded
-size >= L + shift (where the FFT form is also linear).  Bar for a
-reduced-precision form: coefficients within 1e-4 of FP64 (the stated target
-is 1e-3), lags identical except where the FP64 top-two peaks are closer than
-the form's own error, agreement >= 99.9 %.
+They compute the linear correlation over lags 1-shift .. shift directly in
+the time domain (BF16 hi+lo split with three products, or one FP16 product;
+FP32 accumulation), so they are compared with the FP64 oracle and with the
+FP32 FFT form run at a padded size >= L + shift (where the FFT form is also
+linear).  Bar for the three-product form: coefficients within 1e-4 of FP64
+(the stated target is 1e-3), lags identical except where the FP64 top-two
+peaks are closer than the form's own error, agreement >= 99.9 %.  The
+one-product form: within 2e-3.  Lengths whose 64-sample chunk count is not a
+multiple of the MMA group (4 or 2 chunks) take the kernel's tail path.
 """
 import numpy as np
 import pytest
@@ -92,7 +95,8 @@ def test_laggemm_rejects_long_windows(cuda_ok):
         xcorr.xcorr(ev, 300, form="laggemm")
 
 
-@pytest.mark.parametrize("n,c,length,shift", [(300, 1, 1024, 128), (140, 3, 512, 256)])
+@pytest.mark.parametrize("n,c,length,shift", [(300, 1, 1024, 128), (140, 3, 512, 256),
+                                              (37, 1, 300, 50), (150, 3, 600, 200)])
 def test_laggemm_fp16_one_product(cuda_ok, n, c, length, shift):
     """SEISMIC_FORM_LAGGEMM_FP16: one FP16 product per lag sum.  Bar for this
     form: coefficients within 2e-3 of FP64, lags identical where the FP64 top
