@@ -45,6 +45,23 @@ WORKLOAD_TEXT = {
                "one captured CUDA graph (spectra launch + one persistent pair launch per FFT size)",
 }
 CPU_SAMPLE_EVENTS = {"scale": 640, "precision": 1024, "small": 200}
+FORM_TEXT = {"fp32": "FP32 fused FFT form", "fp16": "FP16-spectra fused FFT form",
+             "bf16": "BF16-spectra fused FFT form",
+             "laggemm": "tensor-core lag-GEMM form (BF16 hi/lo, three products, FP32 accumulation)",
+             "laggemm16": "tensor-core lag-GEMM form (FP16 samples scaled by 1/norm, one product, FP32 accumulation)"}
+
+
+def workload_text(workload: str, form: str) -> str:
+    """Workload description with the form that ran it (the lag-GEMM forms use
+    no padded FFT)."""
+    text = WORKLOAD_TEXT[workload]
+    if "FP32 fused FFT form" not in text:
+        return text
+    if form.startswith("laggemm"):
+        text = text.split(", padded FFT")[0]
+    else:
+        text = text.replace(", FP32 fused FFT form", "")
+    return text + ", " + FORM_TEXT.get(form, form)
 
 
 def pair_kernel_name(p: int, c: int) -> str:
@@ -435,7 +452,7 @@ def run_ours(args):
            "warmup": args.warmup, "ms_per_step": step_mean * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": FORM_DTYPE.get(args.form, "f32"),
            "data": "synthetic: seeded family-based waveforms (no public dataset; the reference's is not distributed)",
-           "config": {"workload": args.workload + ": " + WORKLOAD_TEXT[args.workload], "n_events": n,
+           "config": {"workload": args.workload + ": " + workload_text(args.workload, args.form), "n_events": n,
                       "n_channels": c, "event_length": length, "shift": shift, "padded_size": p,
                       "pairs_per_step": npairs, "form": args.form,
                       "l2": "L2 flushed (256 MB write) between timed steps; spectra > L2 for this workload"
