@@ -39,7 +39,8 @@ WORKLOAD_TEXT = {
     "scale": "N=4096 events x 3 channels x L=2048 float32, lags -2047..2048, padded FFT 4096, FP32 fused FFT form",
     "precision": "N=16384 events x 1 channel x L=1024 float32, lags -127..128, padded FFT 2048, FP32 fused FFT form",
     "small": "N=200 events x 1 channel x L=512 float32 (Ricker), lags -511..512, padded FFT 1024, FP32 fused FFT form",
-    "serving": "50,000-event resident catalog x 3 channels x L=1024, lags -255..256, Poisson query stream",
+    "serving": "50,000-event resident catalog x 3 channels x L=1024, lags -255..256, Poisson query stream "
+               "(1..64 events of 256..1024 samples per request)",
     "batched": "256 independent catalogs, N log-uniform in 16..2048, L in {256,512,1000,2048,3000,4096}, "
                "1 or 3 channels, full lag range each, padded FFT = next power of two >= 2L, FP32 fused FFT form, "
                "one captured CUDA graph (spectra launch + one persistent pair launch per FFT size)",
@@ -654,8 +655,8 @@ def run_serving(args):
     srv = Server(cat, shift=shift, form=form, n_slots=4, max_query_events=64, topk=16)
     rng = np.random.default_rng(77)
 
-    def query(nq, seed):
-        return synth.family_catalog(nq, 3, 1024, n_families=1, seed=seed)
+    def query(nq, seed, length=1024):
+        return synth.family_catalog(nq, 3, length, n_families=1, seed=seed)
 
     for k in range(args.warmup):
         srv.wait(srv.submit(query(64, 100 + k)))
@@ -670,7 +671,8 @@ def run_serving(args):
         iso.append(srv.wait(srv.submit(q)).latency_ms)
     iso_wall = time.perf_counter() - t0
     iso_pairs = 64 * n_cat * len(iso)
-    # Poisson load sweep: 1..64 events, full catalog or a station subset of 1,000..50,000
+    # Poisson load sweep: 1..64 events of 256..1024 samples, full catalog or a
+    # station subset of 1,000..50,000
     levels = []
     for rate in (100, 300, 1000):
         n_req = min(48, int(rate * 1.0))
@@ -684,7 +686,8 @@ def run_serving(args):
                 size = int(rng.integers(min(1000, n_cat), n_cat + 1))
                 b = int(rng.integers(0, n_cat - size + 1))
                 e = b + size
-            reqs.append((query(nq, 1000 + rate * 100 + k), (b, e), nq * (e - b)))
+            ql = int(rng.integers(256, 1025))
+            reqs.append((query(nq, 1000 + rate * 100 + k, ql), (b, e), nq * (e - b)))
         tickets = []
         start = time.perf_counter()
         due = start
@@ -715,7 +718,7 @@ def run_serving(args):
            "config": {"workload": "serving: 50,000-event resident catalog x 3 channels x L=1024, lags -255..256, "
                                   f"{form} catalog " + ("16-bit sample planes" if form.startswith("laggemm")
                                                          else "spectra") + " + FP64 norms on device, 4 request "
-                                  "slots, top-16",
+                                  "slots, top-16; Poisson requests of 1..64 events of 256..1024 samples",
                       "n_catalog": n_cat},
            "serving": {"isolated_64_event_full_catalog": {"p50_ms": float(np.percentile(iso, 50)),
                                                           "p99_ms": float(np.percentile(iso, 99)),

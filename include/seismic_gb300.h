@@ -289,6 +289,13 @@ int seismic_server_create(const float *catalog, long long n_catalog, int n_chann
 int seismic_server_submit(seismic_server *server, const float *query, int n_query, long long subset_begin,
                           long long subset_end, float *vals_pos, int *lags_pos, float *vals_neg, int *lags_neg,
                           float *topk_vals, long long *topk_index, long long *ticket);
+/* The same for query events of query_length samples (1 .. event_length):
+ * query is host float32 [n_query][n_channels][query_length], zero-padded to
+ * the catalog's event_length on the device (norms are of the given samples). */
+int seismic_server_submit_len(seismic_server *server, const float *query, int n_query, int query_length,
+                              long long subset_begin, long long subset_end, float *vals_pos, int *lags_pos,
+                              float *vals_neg, int *lags_neg, float *topk_vals, long long *topk_index,
+                              long long *ticket);
 /* Blocks until the ticket's results are in host memory; latency_ms (may be
  * NULL) = submit -> completion. */
 int seismic_server_wait(seismic_server *server, long long ticket, double *latency_ms);

@@ -120,6 +120,7 @@ struct Request {
   long long ticket = 0;
   const float *query = nullptr;
   int n_query = 0;
+  int query_length = 0;  // samples per query row (<= the catalog's L; zero-padded)
   long long col_begin = 0, n_cols = 0;
   float *vp = nullptr, *vn = nullptr;
   int *lp = nullptr, *ln = nullptr;
@@ -255,7 +256,17 @@ int launch_request(seismic_server *s, Request *r) {
   float *d_tv = reinterpret_cast<float *>(base);
   long long *d_ti = reinterpret_cast<long long *>(base + round256((size_t)nq * s->topk * 4));
 
-  cudaError_t e = cudaMemcpyAsync(q_ev, r->query, rows * s->L * sizeof(float), cudaMemcpyHostToDevice, st);
+  // queries of the catalog's length in one copy; shorter ones zero-padded
+  // to it (a pitched copy of query_length samples per row)
+  cudaError_t e;
+  if (r->query_length == s->L) {
+    e = cudaMemcpyAsync(q_ev, r->query, rows * s->L * sizeof(float), cudaMemcpyHostToDevice, st);
+  } else {
+    e = cudaMemsetAsync(q_ev, 0, rows * s->L * sizeof(float), st);
+    if (e == cudaSuccess)
+      e = cudaMemcpy2DAsync(q_ev, (size_t)s->L * sizeof(float), r->query, (size_t)r->query_length * sizeof(float),
+                            (size_t)r->query_length * sizeof(float), rows, cudaMemcpyHostToDevice, st);
+  }
   if (s->lag_form) {  // time-domain lag sums on the tensor cores
     if (e == cudaSuccess)
       e = lag_prepare(q_ev, nq, s->C, s->L, (long long)s->C * s->L, s->L, s->lag_form, q_spec, st);
@@ -476,15 +487,27 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
 extern "C" int seismic_server_submit(seismic_server *s, const float *query, int n_query, long long subset_begin,
                                      long long subset_end, float *vals_pos, int *lags_pos, float *vals_neg,
                                      int *lags_neg, float *topk_vals, long long *topk_index, long long *ticket) {
+  if (!s) return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "null server");
+  return seismic_server_submit_len(s, query, n_query, s->L, subset_begin, subset_end, vals_pos, lags_pos, vals_neg,
+                                   lags_neg, topk_vals, topk_index, ticket);
+}
+
+extern "C" int seismic_server_submit_len(seismic_server *s, const float *query, int n_query, int query_length,
+                                         long long subset_begin, long long subset_end, float *vals_pos,
+                                         int *lags_pos, float *vals_neg, int *lags_neg, float *topk_vals,
+                                         long long *topk_index, long long *ticket) {
   report_status(SEISMIC_OK, "");
   if (!s || !query || !ticket) return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "null argument");
   if (n_query < 1 || n_query > s->max_query)
     return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "query size outside 1..max_query_events");
+  if (query_length < 1 || query_length > s->L)
+    return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "query length outside 1..the catalog's event_length");
   if (subset_begin < 0 || subset_end > s->n_cat || subset_end <= subset_begin)
     return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "catalog subset out of range");
   Request *r = new Request();
   r->query = query;
   r->n_query = n_query;
+  r->query_length = query_length;
   r->col_begin = subset_begin;
   r->n_cols = subset_end - subset_begin;
   r->vp = vals_pos;

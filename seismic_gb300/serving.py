@@ -2,7 +2,8 @@
 seismic_server_* of include/seismic_gb300.h).
 
     srv = Server(catalog, shift=256, form="fp16", n_slots=4, topk=16)
-    t = srv.submit(query_events, subset=(0, 50000))   # returns at once
+    t = srv.submit(query_events, subset=(0, 50000))   # returns at once; events of
+                                                      # any length up to the catalog's
     res = srv.wait(t)                                 # results + latency
 
 Forms: "fp32" / "fp16" (catalog spectra, any lag window), "laggemm" /
@@ -31,6 +32,9 @@ def _declare(lib):
     lib.seismic_server_submit.restype = ctypes.c_int
     lib.seismic_server_submit.argtypes = [vp, vp, ctypes.c_int, ll, ll, vp, vp, vp, vp, vp, vp,
                                           ctypes.POINTER(ll)]
+    lib.seismic_server_submit_len.restype = ctypes.c_int
+    lib.seismic_server_submit_len.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ll, ll, vp, vp, vp, vp, vp, vp,
+                                              ctypes.POINTER(ll)]
     lib.seismic_server_wait.restype = ctypes.c_int
     lib.seismic_server_wait.argtypes = [vp, ll, ctypes.POINTER(ctypes.c_double)]
     lib.seismic_server_stats.restype = ctypes.c_int
@@ -71,11 +75,13 @@ class Server:
         self._live = {}
 
     def submit(self, query: np.ndarray, subset=None) -> int:
+        """query: (n, C, Lq) or (n, Lq) float32 with Lq <= the catalog's event
+        length (shorter events are zero-padded on the device)."""
         import torch
         q = np.ascontiguousarray(query, dtype=np.float32)
         if q.ndim == 2:
             q = q[:, None, :]
-        nq = q.shape[0]
+        nq, ql = q.shape[0], q.shape[-1]
         b, e = subset if subset is not None else (0, self.n_catalog)
         m = nq * (e - b)
         # pinned host buffers keep the device->host copies asynchronous
@@ -85,8 +91,8 @@ class Server:
                 torch.empty(max(1, nq * self.topk), dtype=torch.float32, pin_memory=True),
                 torch.empty(max(1, nq * self.topk), dtype=torch.int64, pin_memory=True)]
         t = ctypes.c_longlong()
-        _lib.check(self.lib.seismic_server_submit(self.handle, qh.data_ptr(), nq, b, e,
-                                                  *(o.data_ptr() for o in outs), ctypes.byref(t)))
+        _lib.check(self.lib.seismic_server_submit_len(self.handle, qh.data_ptr(), nq, ql, b, e,
+                                                      *(o.data_ptr() for o in outs), ctypes.byref(t)))
         self._live[t.value] = (qh, outs, nq, e - b)
         return t.value
 

@@ -241,3 +241,31 @@ def test_precision_workload_size_properties(cuda_ok):
     ag = O.agreement(vp[idx], lp[idx], vn[idx], ln[idx], r)
     assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, ag
     assert ag.lag_mismatch == 0, ag
+
+
+@pytest.mark.parametrize("length", [200, 1000, 4096])
+def test_spectra_norms_fp64_over_amplitude_range(cuda_ok, length):
+    """Kernel (a)'s norms against numpy FP64 sums of squares, for rows from
+    1e-30 to 1e30 in amplitude, a row with one large spike, and a zero row:
+    relative error at the FP64 level, inverse norms rounded once."""
+    import torch
+    from seismic_gb300 import _lib
+    lib = _lib.lib()
+    rng = np.random.default_rng(92)
+    amps = [1e-30, 1e-12, 1e-3, 1.0, 7.5e4, 1e12, 1e30]
+    ev = np.stack([rng.standard_normal(length) * a for a in amps]
+                  + [np.r_[1e20, rng.standard_normal(length - 1) * 1e-3], np.zeros(length)]).astype(np.float32)
+    n = ev.shape[0]
+    p = xcorr.resolve_padded_size(length, length)
+    t = torch.from_numpy(ev).cuda()
+    spec = torch.empty(n * p // 2 * 2, device="cuda")
+    norms = torch.empty(n + (n + 1) // 2, dtype=torch.float64, device="cuda")
+    _lib.check(lib.seismic_spectra_device(t.data_ptr(), n, 1, length, length, length, p, 0, spec.data_ptr(),
+                                          norms.data_ptr(), None))
+    torch.cuda.synchronize()
+    got = norms[:n].cpu().numpy()
+    inv = norms[n:].cpu().numpy().view(np.float32)[:n]
+    want = np.sqrt((ev.astype(np.float64) ** 2).sum(axis=1))
+    np.testing.assert_allclose(got[:-1], want[:-1], rtol=1e-12)
+    assert got[-1] == 0.0 and inv[-1] == 0.0
+    np.testing.assert_array_equal(inv[:-1], (1.0 / got[:-1]).astype(np.float32))

@@ -63,9 +63,10 @@ def test_server_same_result_alone_and_in_the_mix(cuda_ok, form):
         r = np.random.default_rng(seed)
         for _ in range(6):
             nq = int(r.integers(1, 33))
+            ql = int(r.choice([200, 350, 512]))  # query events of different lengths
             b = int(r.integers(0, 300))
             e = int(r.integers(b + 1, 600))
-            t = srv.submit(synth.family_catalog(nq, 3, 512, n_families=1, seed=int(r.integers(1 << 30))), (b, e))
+            t = srv.submit(synth.family_catalog(nq, 3, ql, n_families=1, seed=int(r.integers(1 << 30))), (b, e))
             with lock:
                 tickets.append(t)
 
@@ -83,6 +84,32 @@ def test_server_same_result_alone_and_in_the_mix(cuda_ok, form):
     assert srv.stats()["completed"] == 20
     srv.close()
     del rng
+
+
+@pytest.mark.parametrize("form,tol", [("fp32", 1e-5), ("laggemm16", 2e-3)])
+def test_server_shorter_queries(cuda_ok, form, tol):
+    """Query events shorter than the catalog's are zero-padded on the device:
+    the same results as submitting them padded on the host, and within the
+    form's tolerance of FP64.  Longer ones are rejected."""
+    from seismic_gb300 import _lib
+    from seismic_gb300.serving import Server
+    cat = _catalog()
+    srv = Server(cat, shift=100, form=form, n_slots=2, max_query_events=8, topk=4)
+    short = synth.family_catalog(4, 3, 300, n_families=2, seed=74)
+    padded = np.zeros((4, 3, cat.shape[-1]), np.float32)
+    padded[..., :300] = short
+    a = srv.wait(srv.submit(short, subset=(0, 256)))
+    b = srv.wait(srv.submit(padded, subset=(0, 256)))
+    for f in ("vals_pos", "lags_pos", "vals_neg", "lags_neg"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f))
+    r = _fp64_block(cat, padded, 100, 0, 256)
+    ag = O.agreement(a.vals_pos.ravel(), a.lags_pos.ravel(), a.vals_neg.ravel(), a.lags_neg.ravel(), r,
+                     gap_tol=2 * tol)
+    assert ag.max_err_pos < tol and ag.max_err_neg < tol, ag
+    assert ag.lag_mismatch == 0, ag
+    with pytest.raises(_lib.SeismicError):
+        srv.submit(synth.family_catalog(1, 3, cat.shape[-1] + 1, n_families=1, seed=75))
+    srv.close()
 
 
 def test_server_admission_by_hbm_budget(cuda_ok):
