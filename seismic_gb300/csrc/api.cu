@@ -63,6 +63,7 @@ struct DeviceState {
   const float2 *twiddles = nullptr;
   int *error_flag = nullptr;  // set by kernels whose bounded waits ran out
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // device-to-host copies of the host entry point (made on first use)
   // grow-only cached buffers used when the caller passes none
   void *ws = nullptr;
   size_t ws_bytes = 0;
@@ -72,6 +73,13 @@ struct DeviceState {
 
 static std::mutex g_mutex;
 static std::vector<DeviceState> g_devices;
+
+// Lag-GEMM launches per host call: the device-to-host copy of each chunk's
+// outputs overlaps the next chunk's kernel.
+constexpr int kHostLagChunks = 8;
+
+// Packed index of pair (i, i): where row i of the upper triangle starts.
+static long long packed_row_start(long long i, long long n) { return i * n - i * (i - 1) / 2; }
 
 static int ensure_device(int *dev_out, DeviceState **st_out) {
   int dev = 0;
@@ -486,15 +494,69 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
               "events H2D");
   if (n_classes_hist > 0)
     SEISMIC_TRY(cudaMemsetAsync(d_hist, 0, 2 * (size_t)n_classes_hist * sizeof(int), stream), "hist clear");
-  s = run_xcorr(*st, d_ev, n_events, n_channels, event_length, (long long)n_channels * event_length, event_length,
-                padded_size, shift, threshold, n_classes_hist, d_vp, d_lp, d_vn, d_ln, d_hist,
-                d_hist + (n_classes_hist > 0 ? n_classes_hist : 0), d_ws, stream, form);
-  if (s) return s;
-  const size_t ob = (size_t)npairs * 4;
-  SEISMIC_TRY(cudaMemcpyAsync(vals_pos, d_vp, ob, cudaMemcpyDeviceToHost, stream), "vals_pos D2H");
-  SEISMIC_TRY(cudaMemcpyAsync(lags_pos, d_lp, ob, cudaMemcpyDeviceToHost, stream), "lags_pos D2H");
-  SEISMIC_TRY(cudaMemcpyAsync(vals_neg, d_vn, ob, cudaMemcpyDeviceToHost, stream), "vals_neg D2H");
-  SEISMIC_TRY(cudaMemcpyAsync(lags_neg, d_ln, ob, cudaMemcpyDeviceToHost, stream), "lags_neg D2H");
+  int *d_hmax = d_hist, *d_hmin = d_hist + (n_classes_hist > 0 ? n_classes_hist : 0);
+  if (is_lag_form(form)) {
+    // the lag-GEMM walks the triangle by blocks of rows, whose packed outputs
+    // are contiguous: launch it in chunks and copy each chunk's outputs back
+    // on a second stream while the next chunk runs
+    if (!st->copy_stream)
+      SEISMIC_TRY(cudaStreamCreateWithFlags(&st->copy_stream, cudaStreamNonBlocking), "copy stream");
+    SEISMIC_TRY(lag_prepare(d_ev, n_events, n_channels, event_length, (long long)n_channels * event_length,
+                            event_length, form, d_ws, stream),
+                "lag-GEMM prep");
+    g_launches.fetch_add(1);
+    const long long nblk = lag_blocks(n_events);
+    const int chunks = (int)(nblk < kHostLagChunks ? nblk : kHostLagChunks);
+    float *hv[2] = {vals_pos, vals_neg};
+    int *hl[2] = {lags_pos, lags_neg};
+    float *dv[2] = {d_vp, d_vn};
+    int *dl[2] = {d_lp, d_ln};
+    std::vector<cudaEvent_t> done(chunks, nullptr);
+    int status = SEISMIC_OK;
+    long long b0 = 0;
+    for (int k = 0; k < chunks && status == SEISMIC_OK; ++k) {
+      // chunk k ends where the rows so far hold about (k + 1) / chunks of the pairs
+      const long long target = npairs * (k + 1) / chunks;
+      long long b1 = b0 + 1;
+      while (b1 < nblk && packed_row_start(lag_block_row(b1, n_events), n_events) < target) ++b1;
+      if (k == chunks - 1) b1 = nblk;
+      const long long p0 = packed_row_start(lag_block_row(b0, n_events), n_events);
+      const long long p1 = packed_row_start(lag_block_row(b1, n_events), n_events);
+      cudaError_t e = launch_lag_blocks(d_ws, n_events, n_channels, event_length, shift, threshold, n_classes_hist,
+                                        d_vp, d_lp, d_vn, d_ln, d_hmax, d_hmin, st->error_flag, st->sm_count,
+                                        stream, form, b0, b1);
+      if (e == cudaSuccess) {
+        g_launches.fetch_add(1);
+        e = cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(done[k], stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st->copy_stream, done[k], 0);
+      for (int o = 0; o < 2 && e == cudaSuccess && p1 > p0; ++o) {
+        e = cudaMemcpyAsync(hv[o] + p0, dv[o] + p0, (size_t)(p1 - p0) * 4, cudaMemcpyDeviceToHost, st->copy_stream);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(hl[o] + p0, dl[o] + p0, (size_t)(p1 - p0) * 4, cudaMemcpyDeviceToHost,
+                              st->copy_stream);
+      }
+      if (e != cudaSuccess) status = cuda_status(e, "lag-GEMM chunk");
+      if (b1 >= nblk) break;
+      b0 = b1;
+    }
+    const cudaError_t es = cudaStreamSynchronize(st->copy_stream);
+    for (cudaEvent_t ev : done)
+      if (ev) cudaEventDestroy(ev);
+    if (status) return status;
+    SEISMIC_TRY(es, "copy stream sync");
+  } else {
+    s = run_xcorr(*st, d_ev, n_events, n_channels, event_length, (long long)n_channels * event_length, event_length,
+                  padded_size, shift, threshold, n_classes_hist, d_vp, d_lp, d_vn, d_ln, d_hmax, d_hmin, d_ws, stream,
+                  form);
+    if (s) return s;
+    const size_t ob = (size_t)npairs * 4;
+    SEISMIC_TRY(cudaMemcpyAsync(vals_pos, d_vp, ob, cudaMemcpyDeviceToHost, stream), "vals_pos D2H");
+    SEISMIC_TRY(cudaMemcpyAsync(lags_pos, d_lp, ob, cudaMemcpyDeviceToHost, stream), "lags_pos D2H");
+    SEISMIC_TRY(cudaMemcpyAsync(vals_neg, d_vn, ob, cudaMemcpyDeviceToHost, stream), "vals_neg D2H");
+    SEISMIC_TRY(cudaMemcpyAsync(lags_neg, d_ln, ob, cudaMemcpyDeviceToHost, stream), "lags_neg D2H");
+  }
   std::vector<int> h(n_classes_hist > 0 ? 2 * (size_t)n_classes_hist : 0);
   if (n_classes_hist > 0)
     SEISMIC_TRY(cudaMemcpyAsync(h.data(), d_hist, h.size() * sizeof(int), cudaMemcpyDeviceToHost, stream),

@@ -169,6 +169,16 @@ cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length,
                             long long ch_stride, int shift, float threshold, int n_hist, float *vp, int *lp,
                             float *vn, int *ln, int *hmax, int *hmin, void *ws, int *error_flag, int sm_count,
                             cudaStream_t s, int *launches, int form);
+// The triangle's A-side blocks of 128 events, the first event row of block b
+// (n for b past the end), and a launch over blocks [blk_begin, blk_end) of
+// events already prepared in ws: it writes the packed outputs of rows
+// lag_block_row(blk_begin) .. lag_block_row(blk_end) - 1, a contiguous range.
+long long lag_blocks(long long n);
+long long lag_block_row(long long b, long long n);
+cudaError_t launch_lag_blocks(const void *ws, long long n, int C, int length, int shift, float threshold,
+                              int n_hist, float *vp, int *lp, float *vn, int *ln, int *hmax, int *hmin,
+                              int *error_flag, int sm_count, cudaStream_t s, int form, long long blk_begin,
+                              long long blk_end);
 // Rectangle: queries (prepared in q_ws) x catalog events col_begin ..
 // col_begin + n_cols - 1 (prepared in cat_ws); outputs [n_query][n_cols].
 cudaError_t launch_lag_rect(const void *cat_ws, long long n_cat, const void *q_ws, long long n_query, int C,

@@ -141,6 +141,7 @@ struct LagArgs {
   // lo*hi) or 1 (FP16 hi; hi*hi); the kernel is instantiated per value
   int nhl;
   int kgroup;     // K-chunks per MMA group (1 .. kLagGroupMax, at most stages / 2)
+  long long blk_begin, blk_end;  // triangle: the 128-event blocks this launch walks
 };
 
 struct LagSmem {  // offsets into dynamic shared memory (base 1024-aligned)
@@ -311,7 +312,8 @@ __global__ void __launch_bounds__(kLagThreads, 1)
   // A-side events walked in blocks of 128: the triangle's rows, or the
   // catalog columns col_begin .. col_begin + n_cols - 1 of a rectangle
   const long long a_row0 = RECT ? a.col_begin : 0;
-  const long long nblk = ((RECT ? a.n_cols : N) + kLagM - 1) / kLagM;
+  // A-side blocks [blk_begin, nblk): all of them, or a chunk of the triangle
+  const long long nblk = RECT ? (a.n_cols + kLagM - 1) / kLagM : a.blk_end;
   const long long n_rect = RECT ? a.n_query : 0;
   const long long n_j = RECT ? a.n_query : N;  // j's: triangle events or queries
   const int kchunks = a.lp / kLagKC;
@@ -320,7 +322,7 @@ __global__ void __launch_bounds__(kLagThreads, 1)
   const uint32_t idesc = tc::idesc_f16_f32(kLagM, a.wt, NHL == 1);
   const uint32_t buf_cols = (uint32_t)(a.jp * a.wpad);  // TMEM columns of one pass
 
-  long long b = 0, q = 0;
+  long long b = RECT ? 0 : a.blk_begin, q = 0;
   advance_item(b, q, blockIdx.x, N, a.jc, nblk, n_rect);
 
   if (warp == 4) {
@@ -854,20 +856,22 @@ static cudaError_t launch_lag_kernel(LagArgs &a, const LagPlan &pl, const unsign
   return cudaGetLastError();
 }
 
-cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length, long long ev_stride,
-                            long long ch_stride, int shift, float threshold, int n_hist, float *vp, int *lp,
-                            float *vn, int *ln, int *hmax, int *hmin, void *ws, int *error_flag, int sm_count,
-                            cudaStream_t s, int *launches, int form) {
+long long lag_blocks(long long n) { return (n + kLagM - 1) / kLagM; }
+
+long long lag_block_row(long long b, long long n) { return b * kLagM < n ? b * kLagM : n; }
+
+cudaError_t launch_lag_blocks(const void *ws, long long n, int C, int length, int shift, float threshold,
+                              int n_hist, float *vp, int *lp, float *vn, int *ln, int *hmax, int *hmin,
+                              int *error_flag, int sm_count, cudaStream_t s, int form, long long blk_begin,
+                              long long blk_end) {
   const int nhl = lag_planes(form);
   const LagPlan pl = lag_plan(n, C, length, shift, n_hist, nhl);
-  if (!pl.ok) return cudaErrorInvalidValue;
-  cudaError_t e = lag_prepare(events, n, C, length, ev_stride, ch_stride, form, ws, s);
-  if (e != cudaSuccess) return e;
-  ++*launches;
+  const long long nblk = lag_blocks(n);
+  if (!pl.ok || blk_begin < 0 || blk_end > nblk || blk_begin > blk_end) return cudaErrorInvalidValue;
   const size_t xb = lag_plane_bytes(n, C, pl.lp);
   const unsigned short *xhi = reinterpret_cast<const unsigned short *>(ws);
-  const unsigned short *xlo = nhl > 1 ? reinterpret_cast<const unsigned short *>(reinterpret_cast<char *>(ws) + xb)
-                                      : nullptr;
+  const unsigned short *xlo =
+      nhl > 1 ? reinterpret_cast<const unsigned short *>(reinterpret_cast<const char *>(ws) + xb) : nullptr;
   LagArgs a{};
   a.xhi = xhi;
   a.xlo = xlo;
@@ -887,10 +891,23 @@ cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length,
   a.max_hist = hmax;
   a.min_hist = hmin;
   a.error_flag = error_flag;
-  const long long nblk = (n + kLagM - 1) / kLagM;
+  a.blk_begin = blk_begin;
+  a.blk_end = blk_end;
   long long items = 0;
-  for (long long bb = 0; bb < nblk; ++bb) items += (n - bb * kLagM + pl.jc - 1) / pl.jc;
-  e = launch_lag_kernel(a, pl, xhi, xlo, n * C, items, sm_count, s);
+  for (long long bb = blk_begin; bb < blk_end; ++bb) items += (n - bb * kLagM + pl.jc - 1) / pl.jc;
+  return launch_lag_kernel(a, pl, xhi, xlo, n * C, items, sm_count, s);
+}
+
+cudaError_t launch_lag_gemm(const float *events, long long n, int C, int length, long long ev_stride,
+                            long long ch_stride, int shift, float threshold, int n_hist, float *vp, int *lp,
+                            float *vn, int *ln, int *hmax, int *hmin, void *ws, int *error_flag, int sm_count,
+                            cudaStream_t s, int *launches, int form) {
+  if (!lag_plan(n, C, length, shift, n_hist, lag_planes(form)).ok) return cudaErrorInvalidValue;
+  cudaError_t e = lag_prepare(events, n, C, length, ev_stride, ch_stride, form, ws, s);
+  if (e != cudaSuccess) return e;
+  ++*launches;
+  e = launch_lag_blocks(ws, n, C, length, shift, threshold, n_hist, vp, lp, vn, ln, hmax, hmin, error_flag,
+                        sm_count, s, form, 0, lag_blocks(n));
   if (e == cudaSuccess) ++*launches;
   return e;
 }

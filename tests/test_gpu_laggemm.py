@@ -128,3 +128,16 @@ def test_laggemm_fp16_amplitude_range(cuda_ok, amplitude):
     ag = O.agreement(res.vals_pos, res.lags_pos, res.vals_neg, res.lags_neg, r, gap_tol=2 * tol)
     assert ag.max_err_pos < tol and ag.max_err_neg < tol, ag
     assert ag.lag_mismatch == 0, ag
+
+
+@pytest.mark.parametrize("form", ["laggemm", "laggemm16"])
+def test_laggemm_host_chunks_match_device_call(cuda_ok, form):
+    """The host entry point runs the lag-GEMM in chunks of 128-event blocks
+    (copies of one chunk overlap the next): bit-identical to one device call."""
+    import torch
+    ev = synth.family_catalog(1100, 1, 256, n_families=6, seed=57)
+    host = xcorr.xcorr(ev, 64, threshold=0.05, n_classes_hist=12, form=form)
+    dev = xcorr.xcorr(torch.from_numpy(ev).cuda(), 64, threshold=0.05, n_classes_hist=12, form=form)
+    torch.cuda.synchronize()
+    for f in ("vals_pos", "lags_pos", "vals_neg", "lags_neg", "max_hist", "min_hist"):
+        np.testing.assert_array_equal(getattr(host, f), getattr(dev, f).cpu().numpy())
