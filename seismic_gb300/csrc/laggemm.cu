@@ -229,10 +229,10 @@ __device__ __forceinline__ void lag_mma_group(const uint32_t (&dcol)[2], const u
 #pragma unroll
       for (int cb = 0; cb < NC; ++cb) {
         const uint64_t dbh = dbk + boff[cb];
-        tc::mma_bf16(dcol[cb], dah, dbh, idesc, (ks | t) == 0 ? acc_first : 1u);
+        tc::mma_f16_elect(dcol[cb], dah, dbh, idesc, (ks | t) == 0 ? acc_first : 1u);
         if constexpr (NHL == 2) {  // hi*lo + lo*hi
-          tc::mma_bf16(dcol[cb], dah, dbh + strip_u, idesc, 1u);
-          tc::mma_bf16(dcol[cb], dah + tile_u, dbh, idesc, 1u);
+          tc::mma_f16_elect(dcol[cb], dah, dbh + strip_u, idesc, 1u);
+          tc::mma_f16_elect(dcol[cb], dah + tile_u, dbh, idesc, 1u);
         }
       }
     }
@@ -360,11 +360,13 @@ __global__ void __launch_bounds__(kLagThreads, 1)
     }
   } else if (warp == 5) {
     // ================================================= MMA issuer
-    // One thread issues every MMA, so the loop body is kept to a few adds:
-    // descriptors are built once and advanced by their start-address field
-    // (16-byte units; shared addresses stay below 2^18 bytes, so the field
-    // never carries), and the (j, N-tile) pairs of a pass are a fixed table.
-    if (lane == 0) {
+    // The warp runs the loop converged and one elected lane issues each MMA
+    // and commit (about 6 % faster than a lane-0-only loop).  The loop body
+    // is kept to a few adds: descriptors are built once and advanced by their
+    // start-address field (16-byte units; shared addresses stay below 2^18
+    // bytes, so the field never carries), and the (j, N-tile) pairs of a pass
+    // are a fixed table.
+    {
       int stage = 0;
       uint32_t phase = 0;
       long long unit = 0, pass = 0;  // (pass, channel) strip units; passes
@@ -450,10 +452,10 @@ __global__ void __launch_bounds__(kLagThreads, 1)
                     for (int cb = 0; cb < ncombo; ++cb) {
                       const uint64_t dbh = dbk + (cb == 0 ? boff[0] : boff[1]);
                       const uint32_t d = cb == 0 ? dcol[0] : dcol[1];
-                      tc::mma_bf16(d, dah, dbh, idesc, acc0);
+                      tc::mma_f16_elect(d, dah, dbh, idesc, acc0);
                       if constexpr (NHL == 2) {
-                        tc::mma_bf16(d, dah, dbh + strip_u, idesc, 1u);
-                        tc::mma_bf16(d, dah + tile_u, dbh, idesc, 1u);
+                        tc::mma_f16_elect(d, dah, dbh + strip_u, idesc, 1u);
+                        tc::mma_f16_elect(d, dah + tile_u, dbh, idesc, 1u);
                       }
                     }
                     if (++st == a.stages) st = 0;
@@ -461,20 +463,20 @@ __global__ void __launch_bounds__(kLagThreads, 1)
                 }
               }
               for (int t = 0; t < g; ++t) {
-                tc::mma_commit(&a_empty[stage]);
+                tc::mma_commit_elect(&a_empty[stage]);
                 if (++stage == a.stages) {
                   stage = 0;
                   phase ^= 1;
                 }
               }
             }
-            tc::mma_commit(&hank_empty[hb]);  // this unit's strips are no longer read
+            tc::mma_commit_elect(&hank_empty[hb]);  // this unit's strips are no longer read
           }
-          tc::mma_commit(&tmem_full[tb]);
+          tc::mma_commit_elect(&tmem_full[tb]);
         }
       }
       // every issued MMA has finished before TMEM is freed (bounded)
-      tc::mma_commit(mma_drain);
+      tc::mma_commit_elect(mma_drain);
       tc::mbar_wait(mma_drain, 0, 1u << 20);
     }
   } else if (warp < 4) {

@@ -141,3 +141,37 @@ def test_laggemm_host_chunks_match_device_call(cuda_ok, form):
     torch.cuda.synchronize()
     for f in ("vals_pos", "lags_pos", "vals_neg", "lags_neg", "max_hist", "min_hist"):
         np.testing.assert_array_equal(getattr(host, f), getattr(dev, f).cpu().numpy())
+
+
+def _hist_from_outputs(vp, vn, nh):
+    """The kernel's binning rule (before the threshold) applied to threshold-0
+    outputs: value >= 1 -> last bin, else int(value / float32(1/nh))."""
+    delta = np.float32(1.0 / nh)
+    out = []
+    for v in (vp.astype(np.float32), (-vn).astype(np.float32)):
+        b = np.floor(v / delta).astype(np.int64)
+        b = np.where(v >= 1.0, nh - 1, np.clip(b, 0, nh - 1))
+        out.append(np.bincount(b, minlength=nh))
+    return out
+
+
+@pytest.mark.parametrize("form", ["laggemm", "laggemm16"])
+def test_laggemm_large_histogram_global_atomics(cuda_ok, form):
+    """More classes than the kernel's shared-memory histogram holds (1024):
+    counts go to global atomics and still match the outputs bin by bin."""
+    ev = synth.family_catalog(200, 1, 512, n_families=5, seed=58)
+    nh = 1500
+    res = xcorr.xcorr(ev, 100, threshold=0.0, n_classes_hist=nh, form=form)
+    hmax, hmin = _hist_from_outputs(res.vals_pos, res.vals_neg, nh)
+    np.testing.assert_array_equal(res.max_hist, hmax)
+    np.testing.assert_array_equal(res.min_hist, hmin)
+
+
+@pytest.mark.parametrize("form", ["laggemm", "laggemm16"])
+def test_laggemm_single_event(cuda_ok, form):
+    """N = 1: the one pair (0, 0) peaks at 1 at lag 0."""
+    ev = synth.family_catalog(1, 1, 700, n_families=1, seed=59)
+    res = xcorr.xcorr(ev, 50, threshold=0.0, n_classes_hist=4, form=form)
+    assert res.vals_pos.shape == (1,)
+    assert abs(res.vals_pos[0] - 1.0) < 2e-3 and res.lags_pos[0] == 0
+    assert int(res.max_hist.sum()) == 1
