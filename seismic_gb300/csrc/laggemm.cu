@@ -327,7 +327,8 @@ __global__ void __launch_bounds__(kLagThreads, 1)
 
   if (warp == 4) {
     // ================================================= TMA producer (A tiles)
-    if (lane == 0) {
+    // converged loop; lane 0 issues the expect-tx arrive and the copies
+    {
       int stage = 0;
       uint32_t phase = 0;
       long long it = 0;
@@ -339,11 +340,14 @@ __global__ void __launch_bounds__(kLagThreads, 1)
           for (int c = 0; c < C && !*abort_flag; ++c) {
             for (int kc = 0; kc < kchunks; ++kc, ++it) {
               if (it >= a.stages && !lag_wait(&a_empty[stage], phase ^ 1, abort_flag, a.error_flag)) break;
-              unsigned char *dst = base + L.a + stage * nhl * tile_bytes;
-              tc::mbar_arrive_expect_tx(&a_full[stage], nhl * tile_bytes);
-              const int row = (int)(c * N + a_row0 + bb * kLagM);
-              tc::tma_load_2d(dst, &tm_hi, kc * kLagKC, row, &a_full[stage]);
-              if (nhl > 1) tc::tma_load_2d(dst + tile_bytes, &tm_lo, kc * kLagKC, row, &a_full[stage]);
+              if (lane == 0) {
+                unsigned char *dst = base + L.a + stage * nhl * tile_bytes;
+                tc::mbar_arrive_expect_tx(&a_full[stage], nhl * tile_bytes);
+                const int row = (int)(c * N + a_row0 + bb * kLagM);
+                tc::tma_load_2d(dst, &tm_hi, kc * kLagKC, row, &a_full[stage]);
+                if (nhl > 1) tc::tma_load_2d(dst + tile_bytes, &tm_lo, kc * kLagKC, row, &a_full[stage]);
+              }
+              __syncwarp();
               issued_mask |= 1u << stage;
               last_parity = (last_parity & ~(1u << stage)) | (phase << stage);
               if (++stage == a.stages) {
