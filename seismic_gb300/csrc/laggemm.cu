@@ -13,10 +13,14 @@
 // a strip of (W + L)/8 distinct core matrices -- about 20 KB per event for
 // the whole K range, built once per j in shared memory.
 //
-// FP32 accuracy from BF16 inputs: x = hi + lo with hi = bf16(x),
-// lo = bf16(x - hi); each lag product is hi_i hi_j + hi_i lo_j + lo_i hi_j
-// (three MMAs into the same FP32 accumulator; lo*lo ~ 2^-16 relative is
-// dropped).  Norms and the final normalisation are FP64, as in the FFT form.
+// Two forms (the kernel is instantiated per plane count NHL):
+//  * FP32 accuracy from BF16 inputs: x = hi + lo with hi = bf16(x),
+//    lo = bf16(x - hi); each lag product is hi_i hi_j + hi_i lo_j + lo_i hi_j
+//    (three MMAs into the same FP32 accumulator; lo*lo ~ 2^-16 relative is
+//    dropped);
+//  * one FP16 plane of the samples scaled by 1/norm, one MMA per product.
+// Norms and the final normalisation are FP64, as in the FFT form.  A second
+// mode (RECT) correlates query events with catalog columns for the server.
 //
 // Work: persistent CTAs (one per SM: 512 TMEM columns and ~200 KB of shared
 // memory each) walk items (I-block of 128 events, chunk of `jc` events j >=
@@ -26,9 +30,11 @@
 // 2 jp wpad <= 512, so the strips of the next j are built and the previous
 // pass's accumulators are reduced while the tensor cores run.  Warp roles:
 //   warps 0-3  build the Hankel strips of the next (pass, channel);
-//   warp 4     TMA producer of the A tiles (128 events x 64 samples, hi and
-//              lo, 128-byte swizzle) into a `stages`-deep ring;
-//   warp 5     TMEM allocation and the single MMA-issuing thread;
+//   warp 4     TMA producer of the A tiles (128 events x 64 samples per
+//              plane, 128-byte swizzle) into a `stages`-deep ring;
+//   warp 5     TMEM allocation and the MMA issue: the warp runs converged and
+//              an elected lane issues the MMAs of a group of K-chunks, chunk
+//              by chunk at each 16-sample K offset;
 //   warps 6-9  epilogue: read TMEM (one lane quarter each, lane = event i),
 //              reduce max/min + lags, write outputs.
 // All mbarrier waits are bounded; a wait that runs out raises the shared
