@@ -652,7 +652,7 @@ def run_serving(args):
     shift = 256
     form = args.form if args.form in ("fp32", "fp16", "laggemm", "laggemm16") else "fp16"
     lib = _lib.lib()
-    srv = Server(cat, shift=shift, form=form, n_slots=4, max_query_events=64, topk=16)
+    srv = Server(cat, shift=shift, form=form, n_slots=args.slots, max_query_events=64, topk=16)
     rng = np.random.default_rng(77)
 
     def query(nq, seed, length=1024):
@@ -717,8 +717,8 @@ def run_serving(args):
            "data": "synthetic: seeded family-based waveforms (no public dataset; the reference's is not distributed)",
            "config": {"workload": "serving: 50,000-event resident catalog x 3 channels x L=1024, lags -255..256, "
                                   f"{form} catalog " + ("16-bit sample planes" if form.startswith("laggemm")
-                                                         else "spectra") + " + FP64 norms on device, 4 request "
-                                  "slots, top-16; Poisson requests of 1..64 events of 256..1024 samples",
+                                                         else "spectra") + f" + FP64 norms on device, {args.slots} "
+                                  "request slots, top-16; Poisson requests of 1..64 events of 256..1024 samples",
                       "n_catalog": n_cat},
            "serving": {"isolated_64_event_full_catalog": {"p50_ms": float(np.percentile(iso, 50)),
                                                           "p99_ms": float(np.percentile(iso, 99)),
@@ -788,6 +788,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--n-events", type=int, default=None, help="override N (small profiling cases only)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--slots", type=int, default=4, help="serving: request slots (concurrent requests)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
