@@ -65,8 +65,9 @@ extern "C" {
  * FP16 (BF16) accumulated over channels in FP32, FP32 inverse FFT and scan. */
 #define SEISMIC_FORM_FP16_SPECTRA 1
 #define SEISMIC_FORM_BF16_SPECTRA 3
-/* Time-domain lag sums on the tensor cores (tcgen05), BF16 hi+lo split with
- * three products (hi*hi + hi*lo + lo*hi) accumulated in FP32; linear
+/* Time-domain lag sums on the tensor cores (tcgen05), BF16 hi+lo split of the
+ * samples scaled by 1/norm, three products (hi*hi + hi*lo + lo*hi)
+ * accumulated in FP32; linear
  * correlation (padded_size is not used); needs 2*shift <= 512 and the
  * per-event lag strip to fit in shared memory (event_length up to ~1500 at
  * 2*shift = 256). */

@@ -52,6 +52,7 @@
 #include <cstdlib>
 
 #include "../../include/seismic_gb300.h"
+#include "energy.cuh"
 #include "kernels.cuh"
 #include "tcgen05.cuh"
 #include "tma_host.cuh"
@@ -81,14 +82,20 @@ __global__ void lag_prep_kernel(const float *__restrict__ ev, long long n, int C
   const long long e = row / C;
   const int c = (int)(row % C);
   const float *src = ev + e * ev_stride + (long long)c * ch_stride;
-  double s = 0.0;
-  for (int k = lane; k < L; k += 32) {
-    const double v = src[k];
-    s += v * v;
-  }
+  // energy as exact float-pair sums of power-of-two-scaled samples, FP64
+  // only across the warp (energy.cuh)
+  float m = 0.f;
+  for (int k = lane; k < L; k += 32) m = fmaxf(m, fabsf(src[k]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  const int xe = energy_exponent(m);
+  const EnergyScale sc(xe);
+  float hi = 0.f, lo = 0.f;
+  for (int k = lane; k < L; k += 32) add_square(sc(src[k]), hi, lo);
+  double s = (double)hi + (double)lo;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  const double nrm = sqrt(s);
+  const double nrm = sqrt(ldexp(s, 2 * xe));
   const float scale = prescale ? (nrm > 0.0 ? (float)(1.0 / nrm) : 0.f) : 1.f;
   unsigned short *dh = xhi + ((long long)c * n + e) * lp;
   unsigned short *dl = xlo ? xlo + ((long long)c * n + e) * lp : nullptr;
@@ -743,9 +750,11 @@ static bool make_map(CUtensorMap *m, const void *ptr, long long rows, int lp) {
 // FP16 hi (one product).
 int lag_planes(int form) { return form == SEISMIC_FORM_LAGGEMM_FP16 ? 1 : 2; }
 
-// Samples are scaled by 1/norm before rounding for the multichannel mean, and
-// always for FP16 (whose range, +-65504, raw amplitudes may exceed).
-static int lag_prescaled(int C, int nhl) { return C > 1 || nhl == 1 ? 1 : 0; }
+// Samples are always scaled by 1/norm before rounding to 16 bits: the
+// multichannel mean needs it, FP16's range (+-65504) needs it, and it keeps
+// every lag sum within [-1, 1], so raw amplitudes near the ends of FP32's
+// range cannot overflow or underflow the FP32 accumulators.
+constexpr int kLagPrescaled = 1;
 
 LagPlan lag_plan(long long n_events, int n_channels, int length, int shift, int n_hist, int nhl) {
   LagPlan pl{};
@@ -815,11 +824,11 @@ cudaError_t lag_prepare(const float *events, long long n, int C, int length, lon
   const long long rows = n * C;
   const unsigned grid = (unsigned)((rows + 7) / 8);
   if (nhl == 1)
-    lag_prep_kernel<true><<<grid, 256, 0, s>>>(events, n, C, length, ev_stride, ch_stride, lp, lag_prescaled(C, nhl),
+    lag_prep_kernel<true><<<grid, 256, 0, s>>>(events, n, C, length, ev_stride, ch_stride, lp, kLagPrescaled,
                                                xhi, nullptr, norms);
   else
     lag_prep_kernel<false><<<grid, 256, 0, s>>>(events, n, C, length, ev_stride, ch_stride, lp,
-                                                lag_prescaled(C, nhl), xhi, xlo, norms);
+                                                kLagPrescaled, xhi, xlo, norms);
   return cudaGetLastError();
 }
 
@@ -841,7 +850,7 @@ static cudaError_t launch_lag_kernel(LagArgs &a, const LagPlan &pl, const unsign
   a.xs_len = pl.xs_len;
   a.stages = pl.stages;
   a.kgroup = pl.kgroup;
-  a.prescaled = lag_prescaled(a.C, a.nhl);
+  a.prescaled = kLagPrescaled;
   a.delta_hist = a.n_hist > 0 ? (float)(1.0 / a.n_hist) : 0.f;
   {
     const LagSmem lay = lag_smem_layout(a);

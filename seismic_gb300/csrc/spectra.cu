@@ -15,6 +15,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include "energy.cuh"
 #include "fft_core.cuh"
 #include "kernels.cuh"
 
@@ -52,26 +53,6 @@ __device__ __forceinline__ void store_spectrum(void *base, int stype, long long 
     reinterpret_cast<__nv_bfloat162 *>(base)[idx] = __float22bfloat162_rn(v);
 }
 
-// Energy of a thread's samples without FP64 arithmetic per sample (FP64 runs
-// at 1/64 of the FP32 rate on this GPU): x*x is split exactly into p + pe
-// (FMA), p is added to the running sum `hi` by Knuth's TwoSum, and the
-// rounding errors collect in `lo`.  hi + lo carries about 46 bits, so the
-// FP64 group sum of (double)hi + (double)lo equals an FP64 accumulation to
-// within ~1e-13 relative; the group sum, sqrt and 1/norm are FP64.  The
-// samples come in scaled by a power of two so that x*x can neither overflow
-// nor, for the terms that matter, fall below FP32's normal range.
-// The _rn intrinsics keep the compiler from contracting the products and
-// sums into FMAs, which would break the exact splits.
-__device__ __forceinline__ void add_square(float x, float &hi, float &lo) {
-  const float p = __fmul_rn(x, x);
-  const float pe = fmaf(x, x, -p);  // p + pe == x * x exactly
-  const float s = __fadd_rn(hi, p);
-  const float bb = __fsub_rn(s, hi);
-  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));  // hi + p == s + e exactly
-  hi = s;
-  lo = __fadd_rn(lo, __fadd_rn(e, pe));
-}
-
 template <int G> __device__ __forceinline__ double group_sum_double(double v, double *red, int g, int t) {
 #pragma unroll
   for (int o = (G < 32 ? G : 32) / 2; o > 0; o >>= 1) v += __shfl_xor_sync(group_lane_mask<G>(), v, o);
@@ -105,16 +86,6 @@ template <int G> __device__ __forceinline__ float group_max_float(float v, doubl
     return v;
   }
 }
-
-// Power-of-two exponent e with |x| * 2^-e < 1 for every |x| <= m (0 for
-// m == 0), read from m's exponent bits (subnormal m: e = -126).
-__device__ __forceinline__ int energy_exponent(float m) {
-  if (!(m > 0.f)) return 0;
-  const int biased = (__float_as_int(m) >> 23) & 0xff;
-  return (biased > 0 ? biased : 1) - 126;
-}
-// 2^k as a float for k in [-126, 127].
-__device__ __forceinline__ float exp2_int(int k) { return __int_as_float((127 + k) << 23); }
 
 template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs &a, long long pair_index,
                                                               unsigned char *smem_raw);
@@ -176,14 +147,12 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
   // range), summed as float pairs, the exponent put back in FP64
   const int xea = energy_exponent(group_max_float<G>(ma, red, g, t));
   const int xeb = energy_exponent(group_max_float<G>(mb, red, g, t));
-  // 2^-e as two factors inside FP32's range (e is in [-126, 128])
-  const float sa1 = exp2_int(-xea / 2), sa2 = exp2_int(-xea - (-xea / 2));
-  const float sb1 = exp2_int(-xeb / 2), sb2 = exp2_int(-xeb - (-xeb / 2));
+  const EnergyScale sca(xea), scb(xeb);
   float eah = 0.f, eal = 0.f, ebh = 0.f, ebl = 0.f;
 #pragma unroll
   for (int k = 0; k < 32; ++k) {
-    add_square(__fmul_rn(__fmul_rn(v[k].x, sa1), sa2), eah, eal);
-    add_square(__fmul_rn(__fmul_rn(v[k].y, sb1), sb2), ebh, ebl);
+    add_square(sca(v[k].x), eah, eal);
+    add_square(scb(v[k].y), ebh, ebl);
   }
 #pragma unroll
   for (int half = 0; half < 2; ++half) {

@@ -112,16 +112,18 @@ def test_laggemm_fp16_one_product(cuda_ok, n, c, length, shift):
     assert int(res.max_hist.sum()) == i.size and int(res.min_hist.sum()) == i.size
 
 
-@pytest.mark.parametrize("amplitude", [3e5, 1e-6])
-def test_laggemm_fp16_amplitude_range(cuda_ok, amplitude):
+@pytest.mark.parametrize("form,tol", [("laggemm16", 2e-3), ("laggemm", 1e-4)])
+@pytest.mark.parametrize("amplitude", [3e5, 1e-6, 1e-25, 1e25])
+def test_laggemm_amplitude_range(cuda_ok, form, tol, amplitude):
     """One-channel catalogs far outside FP16's range (max 65504, normal floor
-    6.1e-5): the FP16 planes hold samples scaled by 1/norm, so the result is
-    the same as at unit amplitude."""
-    tol = 2e-3
+    6.1e-5) and near the ends of FP32's: the FP16 planes hold samples scaled
+    by 1/norm, the BF16 planes keep FP32's exponent range, and the norms are
+    exact float-pair sums of power-of-two-scaled samples, so the result is the
+    same as at unit amplitude."""
     n, length, shift = 96, 512, 64
     ev = synth.family_catalog(n, 1, length, n_families=6, seed=7).astype(np.float32)
     ev = (ev / np.abs(ev).max() * amplitude).astype(np.float32)
-    res = xcorr.xcorr(ev, shift, threshold=0.0, n_classes_hist=16, form="laggemm16")
+    res = xcorr.xcorr(ev, shift, threshold=0.0, n_classes_hist=16, form=form)
     i, j = O.triu_pairs(n)
     r = O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(length, shift))
     assert np.all(np.isfinite(res.vals_pos)) and np.all(np.isfinite(res.vals_neg))
