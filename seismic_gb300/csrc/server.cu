@@ -19,6 +19,7 @@
 // Results do not depend on what else is in flight: every request has its own
 // buffers and the kernels are deterministic.
 #include <chrono>
+#include <cstdlib>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -151,6 +152,12 @@ struct seismic_server {
   const float2 *tw = nullptr;
   int *error_flag = nullptr;  // device flag set by a bounded wait that ran out
   int max_query = 64;
+  // A request joins others already on the device only when at least this
+  // many requests wait (counting it): at light load each request runs alone
+  // (lowest latency), under backlog they overlap (highest throughput).
+  // SEISMIC_SERVER_OVERLAP_BACKLOG, default 2; 1 overlaps whenever a slot
+  // is free.
+  int overlap_backlog = 2;
   // pool
   char *pool = nullptr;
   size_t pool_bytes = 0;
@@ -343,13 +350,15 @@ void dispatcher_main(seismic_server *s, int device) {
     // admit in arrival order; a request that does not fit lets later ones try
     admitted.clear();
     for (auto it = s->pending.begin(); it != s->pending.end();) {
-      int slot = -1;
-      for (size_t k = 0; k < s->slot_busy.size(); ++k)
-        if (!s->slot_busy[k]) {
+      int slot = -1, busy = 0;
+      for (size_t k = 0; k < s->slot_busy.size(); ++k) {
+        if (s->slot_busy[k])
+          ++busy;
+        else if (slot < 0)
           slot = (int)k;
-          break;
-        }
+      }
       if (slot < 0) break;
+      if (busy > 0 && (long long)s->pending.size() < s->overlap_backlog) break;  // wait for the device
       Request *r = *it;
       size_t off = 0;
       if (!pool_alloc(s, r->bytes, &off)) {
@@ -421,6 +430,10 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   s->tw = tw;
   s->error_flag = ef;
   s->max_query = max_query_events;
+  if (const char *env = getenv("SEISMIC_SERVER_OVERLAP_BACKLOG")) {
+    const int v = atoi(env);
+    if (v >= 1) s->overlap_backlog = v;
+  }
   const long long rows = n_catalog * n_channels;
   float *d_cat = nullptr;
   cudaError_t e = cudaSuccess;
