@@ -145,13 +145,19 @@ template <int DIR> __device__ __forceinline__ float2 twiddle_lookup(const float2
 
 // v[r] *= w^r, r = 1..R-1, w = exp(DIR 2 pi i m / (NS R)); powers from one
 // table entry and a shallow product tree (at most 4 roundings per power).
-template <int R> __device__ __forceinline__ void apply_root_powers(float2 *v, float2 w1) {
-  float2 w[R];
+template <int R> __device__ __forceinline__ void root_powers(float2 w1, float2 (&w)[R]) {
   w[1] = w1;
 #pragma unroll
   for (int r = 2; r < R; ++r) w[r] = (r & 1) ? cmul(w[r - 1], w1) : cmul(w[r / 2], w[r / 2]);
+}
+template <int R> __device__ __forceinline__ void apply_powers(float2 *v, const float2 (&w)[R]) {
 #pragma unroll
   for (int r = 1; r < R; ++r) v[r] = cmul(v[r], w[r]);
+}
+template <int R> __device__ __forceinline__ void apply_root_powers(float2 *v, float2 w1) {
+  float2 w[R];
+  root_powers<R>(w1, w);
+  apply_powers<R>(v, w);
 }
 
 template <int P, int R, int NS, int DIR>
@@ -235,14 +241,25 @@ __device__ __forceinline__ void pass_compute(float2 (&v)[32], int t, const float
                                              const float2 *roots = nullptr) {
   constexpr int G = P / 32;
   constexpr int J = 32 / R;
+  if constexpr (NS > 1 && J > 1 && G % NS == 0) {
+    // every job of this thread has the same m = t mod NS: one set of powers
+    float2 w[R];
+    root_powers<R>(roots != nullptr ? roots[0] : twiddle_lookup<DIR>(tw, (t % NS) * (kMaxP / (NS * R))), w);
 #pragma unroll
-  for (int q = 0; q < J; ++q) {
-    const int j = t + q * G;
-    if (roots != nullptr)
-      apply_root_powers<R>(&v[q * R], roots[q]);
-    else
-      apply_twiddles<P, R, NS, DIR>(&v[q * R], j % NS, tw);
-    dft<R, DIR>(&v[q * R]);
+    for (int q = 0; q < J; ++q) {
+      apply_powers<R>(&v[q * R], w);
+      dft<R, DIR>(&v[q * R]);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < J; ++q) {
+      const int j = t + q * G;
+      if (roots != nullptr)
+        apply_root_powers<R>(&v[q * R], roots[q]);
+      else
+        apply_twiddles<P, R, NS, DIR>(&v[q * R], j % NS, tw);
+      dft<R, DIR>(&v[q * R]);
+    }
   }
 }
 
