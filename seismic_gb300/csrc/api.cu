@@ -74,9 +74,9 @@ struct DeviceState {
 static std::mutex g_mutex;
 static std::vector<DeviceState> g_devices;
 
-// Lag-GEMM launches per host call: the device-to-host copy of each chunk's
+// Pair launches per host call: the device-to-host copy of each chunk's
 // outputs overlaps the next chunk's kernel.
-constexpr int kHostLagChunks = 8;
+constexpr int kHostChunks = 8;
 
 // Packed index of pair (i, i): where row i of the upper triangle starts.
 static long long packed_row_start(long long i, long long n) { return i * n - i * (i - 1) / 2; }
@@ -223,7 +223,7 @@ long long pair_work_total(int P, const PairArgs &a) {
 cudaError_t launch_pair_work(int P, const PairArgs &a, int sm_count, int ctas_per_sm, cudaStream_t stream) {
   if (a.couple_end <= a.couple_begin) return cudaSuccess;
   if (staged_supported(P, a)) return launch_pairs_staged(P, a, sm_count, stream);
-  PairArgs d = a;  // direct form: L2 column bands of tiles (triangle mode)
+  PairArgs d = a;  // direct form: L2 row bands of tiles (triangle mode)
   if (!d.rect && d.band_tiles == 0) d.band_tiles = l2_band_tiles(d.n_channels, P, d.stype ? 4 : 8, d.tile);
   static int ctas_cache[16] = {0};
   const int lp2 = 31 - __builtin_clz((unsigned)P);
@@ -235,6 +235,38 @@ cudaError_t launch_pair_work(int P, const PairArgs &a, int sm_count, int ctas_pe
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
   return launch_pairs(P, d, (int)grid, stream);
+}
+
+// Row bands of the pair form launch_pair_work runs on the triangle of these
+// spectra: tile side, work items per tile, tiles per side and tile rows per
+// band, computed as the kernels compute them.
+struct PairBandPlan {
+  long long tile_side, items_per_tile, nb, band;
+};
+static PairBandPlan pair_band_plan(int P, const void *spectra, int stype, long long n, int C) {
+  PairArgs a{};
+  a.spectra = spectra;
+  a.stype = stype;
+  a.n_events = n;
+  a.n_channels = C;
+  a.tile = tune_lookup(P, C).tile;
+  PairBandPlan b{};
+  if (staged_supported(P, a)) {
+    b.tile_side = staged_tile_side(P, a);
+    b.items_per_tile = b.tile_side;
+  } else {
+    b.tile_side = a.tile;
+    b.items_per_tile = (long long)a.tile * a.tile / 2;
+  }
+  b.nb = (n + b.tile_side - 1) / b.tile_side;
+  b.band = l2_band_tiles(C, P, stype ? 4 : 8, (int)b.tile_side);
+  return b;
+}
+// First event row of band k (n past the last band).
+static long long band_row(const PairBandPlan &b, long long k, long long n) {
+  const long long band = (b.band <= 0 || b.band > b.nb) ? b.nb : b.band;
+  const long long r = k * band * b.tile_side;
+  return r < n ? r : n;
 }
 
 int device_context(int *sm_count, const float2 **twiddles, int **error_flag) {
@@ -506,7 +538,7 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
                 "lag-GEMM prep");
     g_launches.fetch_add(1);
     const long long nblk = lag_blocks(n_events);
-    const int chunks = (int)(nblk < kHostLagChunks ? nblk : kHostLagChunks);
+    const int chunks = (int)(nblk < kHostChunks ? nblk : kHostChunks);
     float *hv[2] = {vals_pos, vals_neg};
     int *hl[2] = {lags_pos, lags_neg};
     float *dv[2] = {d_vp, d_vn};
@@ -547,15 +579,64 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
     if (status) return status;
     SEISMIC_TRY(es, "copy stream sync");
   } else {
-    s = run_xcorr(*st, d_ev, n_events, n_channels, event_length, (long long)n_channels * event_length, event_length,
-                  padded_size, shift, threshold, n_classes_hist, d_vp, d_lp, d_vn, d_ln, d_hmax, d_hmin, d_ws, stream,
-                  form);
+    // FFT forms: the pair kernels walk the triangle in L2 row bands, whose
+    // outputs are contiguous packed rows: launch them in chunks of bands
+    // and copy each chunk back on a second stream while the next one runs
+    const long long rows_total = n_events * n_channels;
+    const int stype = form_stype(form);
+    const int prescale = (n_channels > 1 || stype != 0) ? 1 : 0;
+    void *spectra = d_ws;
+    double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(d_ws) + spectra_bytes(rows_total, padded_size,
+                                                                                            stype));
+    s = run_spectra(*st, d_ev, n_events, n_channels, event_length, (long long)n_channels * event_length, event_length,
+                    padded_size, prescale, spectra, norms, stream, stype);
     if (s) return s;
-    const size_t ob = (size_t)npairs * 4;
-    SEISMIC_TRY(cudaMemcpyAsync(vals_pos, d_vp, ob, cudaMemcpyDeviceToHost, stream), "vals_pos D2H");
-    SEISMIC_TRY(cudaMemcpyAsync(lags_pos, d_lp, ob, cudaMemcpyDeviceToHost, stream), "lags_pos D2H");
-    SEISMIC_TRY(cudaMemcpyAsync(vals_neg, d_vn, ob, cudaMemcpyDeviceToHost, stream), "vals_neg D2H");
-    SEISMIC_TRY(cudaMemcpyAsync(lags_neg, d_ln, ob, cudaMemcpyDeviceToHost, stream), "lags_neg D2H");
+    const PairBandPlan bp = pair_band_plan(padded_size, spectra, stype, n_events, n_channels);
+    const long long bands = band_count(bp.nb, bp.band);
+    const int chunks = (int)(bands < kHostChunks ? bands : kHostChunks);
+    if (!st->copy_stream)
+      SEISMIC_TRY(cudaStreamCreateWithFlags(&st->copy_stream, cudaStreamNonBlocking), "copy stream");
+    std::vector<cudaEvent_t> done(chunks > 0 ? chunks : 0, nullptr);
+    int status = SEISMIC_OK;
+    long long k0 = 0;
+    for (int k = 0; k < chunks && status == SEISMIC_OK; ++k) {
+      // chunk k ends at the first band boundary holding >= (k + 1) / chunks of the pairs
+      const long long target = npairs * (k + 1) / chunks;
+      long long k1 = k0 + 1;
+      while (k1 < bands && packed_row_start(band_row(bp, k1, n_events), n_events) < target) ++k1;
+      if (k == chunks - 1) k1 = bands;
+      const long long r0 = band_row(bp, k0, n_events), r1 = band_row(bp, k1, n_events);
+      const long long p0 = packed_row_start(r0, n_events), p1 = packed_row_start(r1, n_events);
+      s = run_pairs(*st, spectra, norms, n_events, n_channels, padded_size, prescale, shift, threshold,
+                    n_classes_hist, d_vp, d_lp, d_vn, d_ln, d_hmax, d_hmin, stream, stype,
+                    band_first_tile(k0, bp.nb, bp.band) * bp.items_per_tile,
+                    band_first_tile(k1, bp.nb, bp.band) * bp.items_per_tile);
+      if (s) {
+        status = s;
+        break;
+      }
+      cudaError_t e = cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
+      if (e == cudaSuccess) e = cudaEventRecord(done[k], stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st->copy_stream, done[k], 0);
+      float *hv[2] = {vals_pos, vals_neg};
+      int *hl[2] = {lags_pos, lags_neg};
+      float *dv[2] = {d_vp, d_vn};
+      int *dl[2] = {d_lp, d_ln};
+      for (int o = 0; o < 2 && e == cudaSuccess && p1 > p0; ++o) {
+        e = cudaMemcpyAsync(hv[o] + p0, dv[o] + p0, (size_t)(p1 - p0) * 4, cudaMemcpyDeviceToHost, st->copy_stream);
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(hl[o] + p0, dl[o] + p0, (size_t)(p1 - p0) * 4, cudaMemcpyDeviceToHost,
+                              st->copy_stream);
+      }
+      if (e != cudaSuccess) status = cuda_status(e, "pair chunk copy");
+      if (k1 >= bands) break;
+      k0 = k1;
+    }
+    const cudaError_t es = cudaStreamSynchronize(st->copy_stream);
+    for (cudaEvent_t ev : done)
+      if (ev) cudaEventDestroy(ev);
+    if (status) return status;
+    SEISMIC_TRY(es, "copy stream sync");
   }
   std::vector<int> h(n_classes_hist > 0 ? 2 * (size_t)n_classes_hist : 0);
   if (n_classes_hist > 0)

@@ -188,7 +188,7 @@ extern "C" int seismic_batch_create(const seismic_catalog *catalogs, int n_catal
     pa.max_hist = c.max_hist;
     pa.min_hist = c.min_hist;
     pa.tile = te.tile;
-    pa.band_tiles = l2_band_tiles(C, P, 8, te.tile);  // L2 column bands, as the single-catalog launch
+    pa.band_tiles = l2_band_tiles(C, P, 8, te.tile);  // L2 row bands, as the single-catalog launch
     pa.twiddles = tw;
     pa.couple_begin = 0;
     pa.couple_end = pair_couples_total(c.n_events, te.tile);

@@ -83,18 +83,32 @@ struct PairArgs {
   int *error_flag;
 };
 
-// Tile columns per L2 band of the triangle walk (PairArgs::band_tiles) so
-// that one band of j spectra takes about 48 MB of L2.
+// Tile rows per L2 band of the triangle walk (PairArgs::band_tiles) so
+// that the spectra of one band's events take about 48 MB of L2.
 inline int l2_band_tiles(long long n_channels, int P, int elem_bytes, int tile) {
   const long long ev_bytes = n_channels * (P / 2) * (long long)elem_bytes;
   const long long band_events = (48ll << 20) / (ev_bytes > 0 ? ev_bytes : 1);
   return (int)(band_events / tile > 1 ? band_events / tile : 1);
 }
 
+// Row bands of the triangle walk (band_tile, pair_core.cuh): the number of bands, and the first tile index and
+// first tile row of band k (k == bands: the totals).
+__host__ __device__ __forceinline__ long long band_count(long long nb, long long band) {
+  if (band <= 0 || band > nb) band = nb;
+  return nb > 0 ? (nb + band - 1) / band : 0;
+}
+__host__ __device__ __forceinline__ long long band_first_tile(long long k, long long nb, long long band) {
+  if (band <= 0 || band > nb) band = nb;
+  long long r0 = k * band < nb ? k * band : nb;
+  // tiles in rows 0 .. r0 - 1 of the upper triangle
+  return r0 * nb - r0 * (r0 - 1) / 2;
+}
+
 // ---- staged pair form (pairs_staged.cu): spectra staged into shared memory
 // by TMA (P = 4096 by default).  Work items are (event i, T consecutive j).
 bool staged_supported(int P, const PairArgs &a);
 long long staged_items_total(int P, const PairArgs &a);  // triangle or rectangle
+int staged_tile_side(int P, const PairArgs &a);         // T: events per tile side (items per tile)
 // Launches items [a.couple_begin, a.couple_end) of the staged decomposition.
 cudaError_t launch_pairs_staged(int P, const PairArgs &a, int sm_count, cudaStream_t s);
 

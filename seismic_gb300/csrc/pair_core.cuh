@@ -51,42 +51,44 @@ __device__ __forceinline__ void decode_tile(long long x, long long nb, long long
   bj = b + (x - tri_start(b, nb));
 }
 
-// Tile x of the upper triangle of nb x nb tiles in column-band order: bands
-// of `band` tile columns (band <= 0: one band, i.e. plain row-major), each
-// walked row by row from the top row down to its own diagonal, so the
-// columns of one band stay in L2 while every row above it passes over them.
+// Tile x of the upper triangle of nb x nb tiles in row-band order: bands of
+// `band` tile rows (band <= 0: one band), each walked column by column from
+// its own diagonal to the right edge, top to bottom within a column.  The
+// rows of one band (its i spectra) stay in L2 while every column to their
+// right passes over them once, and the outputs of one band are the packed
+// rows of its events: a contiguous range of the packed triangle.
 __host__ __device__ __forceinline__ void band_tile(long long x, long long nb, long long band, long long &bi,
                                                    long long &bj) {
   if (band <= 0 || band > nb) band = nb;
-  long long b0 = 0;  // first tile column of the band
+  long long r0 = 0;  // first tile row of the band
   for (;;) {
-    const long long be = b0 + band < nb ? b0 + band : nb;
-    const long long wb = be - b0;
-    const long long cnt = b0 * wb + wb * (wb + 1) / 2;
-    if (x < cnt || be >= nb) {
-      if (x < b0 * wb) {  // rows above the band: full width
+    const long long re = r0 + band < nb ? r0 + band : nb;
+    const long long wb = re - r0;
+    const long long tri = wb * (wb + 1) / 2;
+    const long long cnt = tri + wb * (nb - re);
+    if (x < cnt || re >= nb) {
+      if (x < tri) {  // the band's own triangle: column c holds c + 1 tiles
+        long long c = (long long)((sqrtf(8.0f * (float)x + 1.0f) - 1.0f) * 0.5f);
+        if (c < 0) c = 0;
+        if (c > wb - 1) c = wb - 1;
+        while (c + 1 < wb && (c + 1) * (c + 2) / 2 <= x) ++c;
+        while (c > 0 && c * (c + 1) / 2 > x) --c;
+        bi = r0 + (x - c * (c + 1) / 2);
+        bj = r0 + c;
+      } else {        // full columns right of the band, wb tiles each
+        const long long y = x - tri;
         // 32-bit division when it fits (a 64-bit one is a long software routine)
-        bi = (x < 0x7fffffffLL && wb < 0x7fffffffLL) ? (long long)((unsigned)x / (unsigned)wb) : x / wb;
-        bj = b0 + (x - bi * wb);
-      } else {            // the band's own triangle
-        long long r, c;
-#ifdef __CUDA_ARCH__
-        decode_tile(x - b0 * wb, wb, r, c);
-#else
-        const long long xx = x - b0 * wb;
-        r = 0;
-        while (tri_start(r + 1, wb) <= xx) ++r;
-        c = r + (xx - tri_start(r, wb));
-#endif
-        bi = b0 + r;
-        bj = b0 + c;
+        const long long q = (y < 0x7fffffffLL && wb < 0x7fffffffLL) ? (long long)((unsigned)y / (unsigned)wb) : y / wb;
+        bj = re + q;
+        bi = r0 + (y - q * wb);
       }
       return;
     }
     x -= cnt;
-    b0 = be;
+    r0 = re;
   }
 }
+
 
 // Spectrum storage types: 0 float2 (FP32 form), 1 half2, 2 bfloat162.  For
 // the half types the pointwise product a * conj(b) runs in the storage type

@@ -11,8 +11,8 @@
 // or product spectrum ever written to global memory.
 //
 // Work decomposition.  Events are cut into square tiles of `tile` events;
-// tiles (bi, bj >= bi) of the upper triangle are enumerated in column bands
-// of `band_tiles` tiles (band_tile; 0 = plain row-major).  A tile holds tile*tile/2 couples (pair_core.cuh); couples
+// tiles (bi, bj >= bi) of the upper triangle are enumerated in row bands
+// of `band_tiles` tile rows (band_tile; 0 = one band).  A tile holds tile*tile/2 couples (pair_core.cuh); couples
 // are dealt to groups of G = P/32 threads round-robin, the groups of one CTA
 // taking neighbouring couples of the same tile, whose spectra they read
 // straight from global memory (L2).  This form serves every size P and the

@@ -9,10 +9,11 @@
 // j0 .. j0+T-1; group g of the CTA's NG FFT groups takes the couple
 // (i; j0+2g, j0+2g+1) -- the same couples as the direct form, so both forms
 // give bit-identical results.  The items of the upper triangle are square
-// tiles of T x T events (T items per tile, one per i), walked in column
-// bands of `band_tiles` tiles so the j spectra of a band stay in L2 while
-// every row above the band passes over it; the rectangle (query x catalog)
-// walks column blocks, all queries per block.
+// tiles of T x T events (T items per tile, one per i), walked in row bands
+// of `band_tiles` tile rows so the i spectra of a band stay in L2 while
+// every column to its right passes over it once (and a band's outputs are
+// contiguous packed rows); the rectangle (query x catalog) walks column
+// blocks, all queries per block.
 //
 // Pipeline.  Each item's spectra are cut into units (channel c, chunk r):
 // bins [r S, (r+1) S) of row i and of the T rows j0..j0+T-1, exactly the
@@ -315,8 +316,10 @@ bool staged_supported(int P, const PairArgs &a) {
   return tensor_map_encoder() != nullptr;
 }
 
+int staged_tile_side(int P, const PairArgs &a) { return 2 * (staged_nwarp(P, a.stype, a.n_channels) * 32 / (P / 32)); }
+
 long long staged_items_total(int P, const PairArgs &a) {
-  const long long T = 2 * (staged_nwarp(P, a.stype, a.n_channels) * 32 / (P / 32));
+  const long long T = staged_tile_side(P, a);
   if (a.rect) return a.n_query * ((a.n_cols + T - 1) / T);
   const long long nb = (a.n_events + T - 1) / T;
   return T * (nb * (nb + 1) / 2);

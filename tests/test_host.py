@@ -71,25 +71,40 @@ def test_packed_index():
 
 def _band_tile(x, nb, band):
     """Python restatement of band_tile (pair_core.cuh): tile x of the upper
-    triangle of nb x nb tiles in column bands of `band` tiles (0 = one band,
-    plain row-major)."""
+    triangle of nb x nb tiles in row bands of `band` tiles (0 = one band),
+    each band column by column from its diagonal, top to bottom."""
     band = band if 0 < band <= nb else nb
-    b0 = 0
+    r0 = 0
     while True:
-        be = min(b0 + band, nb)
-        wb = be - b0
-        cnt = b0 * wb + wb * (wb + 1) // 2
-        if x < cnt or be >= nb:
-            if x < b0 * wb:
-                bi, bj = divmod(x, wb)
-                return bi, bj + b0
-            xx = x - b0 * wb
-            r = 0
-            while (r + 1) * wb - (r + 1) * r // 2 <= xx:
-                r += 1
-            return b0 + r, b0 + r + (xx - (r * wb - r * (r - 1) // 2))
+        re = min(r0 + band, nb)
+        wb = re - r0
+        tri = wb * (wb + 1) // 2
+        cnt = tri + wb * (nb - re)
+        if x < cnt or re >= nb:
+            if x < tri:
+                c = 0
+                while (c + 1) * (c + 2) // 2 <= x:
+                    c += 1
+                return r0 + (x - c * (c + 1) // 2), r0 + c
+            q, rem = divmod(x - tri, wb)
+            return r0 + rem, re + q
         x -= cnt
-        b0 = be
+        r0 = re
+
+
+@pytest.mark.parametrize("nb,band", [(1, 0), (7, 0), (7, 3), (12, 5), (30, 4), (30, 30), (9, 1)])
+def test_row_bands_are_contiguous_rows(nb, band):
+    """Tiles of row band k are the consecutive tile indices from
+    band_first_tile(k) (rows 0 .. r0 - 1 of the triangle before it) and hold
+    exactly the tile rows of the band: the band's outputs are a contiguous
+    range of packed rows (what the host entry point copies chunk by chunk)."""
+    b = band if 0 < band <= nb else nb
+    bands = (nb + b - 1) // b
+    first = [min(k * b, nb) * nb - min(k * b, nb) * (min(k * b, nb) - 1) // 2 for k in range(bands + 1)]
+    assert first[-1] == nb * (nb + 1) // 2
+    for k in range(bands):
+        rows = {_band_tile(x, nb, band)[0] for x in range(first[k], first[k + 1])}
+        assert rows == set(range(k * b, min((k + 1) * b, nb)))
 
 
 def _scheduler_pairs(n, tile, band=0):
