@@ -284,12 +284,12 @@ constexpr int kStagedWarps = 12;  // FFT warps per CTA, plus the producer warp
 // in whole groups of P/32 threads.
 constexpr int staged_wide_warps(int P) { return P >= 4096 ? 12 : (P == 2048 ? 14 : 15); }
 
-// FFT warps the dispatch uses.  The wide CTA (more FFT warps, a ring of
-// 2-chunk slots) wins where one channel's item fits its smaller ring: FP32
-// spectra, one channel, P = 2048 (263 vs 230 M pairs/s measured; with three
-// channels 175 vs 184).  SEISMIC_STAGED_WARPS=wide / =12 forces either.
+// FFT warps the dispatch uses.  The wide CTA (more FFT warps, a smaller
+// ring) wins where one channel's item fits it: one channel at P = 2048 (FP32
+// spectra 263 vs 230 M pairs/s measured, FP16 256 vs 233, BF16 255 vs 237;
+// with three channels 175 vs 184).  SEISMIC_STAGED_WARPS=wide / =12 forces
+// either.
 static int staged_nwarp(int P, int stype, int n_channels) {
-  if (stype != 0) return kStagedWarps;
   const char *e = getenv("SEISMIC_STAGED_WARPS");
   if (e && strcmp(e, "wide") == 0) return staged_wide_warps(P);
   if (e && strcmp(e, "12") == 0) return kStagedWarps;
@@ -374,8 +374,13 @@ template <int P> static cudaError_t launch_staged_p(const PairArgs &a, int sm_co
       if (staged_nwarp(P, 0, a.n_channels) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 2, 0>(a, sm_count, s);
       return staged_ru() == 2 ? launch_staged_t<P, kStagedWarps, 2, 0>(a, sm_count, s)
                               : launch_staged_t<P, kStagedWarps, 4, 0>(a, sm_count, s);
-    case 1: return launch_staged_t<P, kStagedWarps, 4, 1>(a, sm_count, s);
-    case 2: return launch_staged_t<P, kStagedWarps, 4, 2>(a, sm_count, s);
+    // half-precision spectra: half the ring bytes, so the wide CTA keeps 4-chunk slots
+    case 1:
+      if (staged_nwarp(P, 1, a.n_channels) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 4, 1>(a, sm_count, s);
+      return launch_staged_t<P, kStagedWarps, 4, 1>(a, sm_count, s);
+    case 2:
+      if (staged_nwarp(P, 2, a.n_channels) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 4, 2>(a, sm_count, s);
+      return launch_staged_t<P, kStagedWarps, 4, 2>(a, sm_count, s);
     default: return cudaErrorInvalidValue;
   }
 }
