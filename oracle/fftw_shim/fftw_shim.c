@@ -17,6 +17,7 @@
  *
  * Every execute call is re-entrant: the only state is the read-only plan.
  */
+#define _POSIX_C_SOURCE 200112L /* posix_memalign under -std=c11 */
 #include "fftw3.h"
 
 #include <math.h>
