@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 namespace seismic {
@@ -84,10 +85,16 @@ struct PairArgs {
 };
 
 // Tile rows per L2 band of the triangle walk (PairArgs::band_tiles) so
-// that the spectra of one band's events take about 48 MB of L2.
+// that the spectra of one band's events take about 48 MB of L2
+// (SEISMIC_L2_BAND_MB sets another size, 1 .. 4096 MB).
 inline int l2_band_tiles(long long n_channels, int P, int elem_bytes, int tile) {
+  long long band_mb = 48;
+  if (const char *env = getenv("SEISMIC_L2_BAND_MB")) {
+    const long long v = atoll(env);
+    if (v >= 1 && v <= 4096) band_mb = v;
+  }
   const long long ev_bytes = n_channels * (P / 2) * (long long)elem_bytes;
-  const long long band_events = (48ll << 20) / (ev_bytes > 0 ? ev_bytes : 1);
+  const long long band_events = (band_mb << 20) / (ev_bytes > 0 ? ev_bytes : 1);
   return (int)(band_events / tile > 1 ? band_events / tile : 1);
 }
 
