@@ -26,6 +26,16 @@ __device__ __forceinline__ void add_square(float x, float &hi, float &lo) {
   lo = __fadd_rn(lo, __fadd_rn(e, pe));
 }
 
+// (hi, lo) += (h2, l2): the high parts by TwoSum, the rounding error and the
+// low parts into lo.
+__device__ __forceinline__ void add_pair(float &hi, float &lo, float h2, float l2) {
+  const float s = __fadd_rn(hi, h2);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+  hi = s;
+  lo = __fadd_rn(lo, __fadd_rn(l2, e));
+}
+
 // Power-of-two exponent e with |x| * 2^-e < 1 for every |x| <= m (0 for
 // m == 0), read from m's exponent bits (subnormal m: e = -125).
 __device__ __forceinline__ int energy_exponent(float m) {

@@ -53,24 +53,31 @@ __device__ __forceinline__ void store_spectrum(void *base, int stype, long long 
     reinterpret_cast<__nv_bfloat162 *>(base)[idx] = __float22bfloat162_rn(v);
 }
 
-template <int G> __device__ __forceinline__ double group_sum_double(double v, double *red, int g, int t) {
+// Sum over the group of G threads of float pairs (hi, lo) by exact TwoSum
+// steps (energy.cuh): the group's energy without FP64 shuffles.  `red` is
+// the group's scratch (2 * ceil(G / 32) doubles); thread 0's result is the
+// one used.
+template <int G> __device__ __forceinline__ void group_sum_pair(float &hi, float &lo, double *red, int g, int t) {
 #pragma unroll
-  for (int o = (G < 32 ? G : 32) / 2; o > 0; o >>= 1) v += __shfl_xor_sync(group_lane_mask<G>(), v, o);
+  for (int o = (G < 32 ? G : 32) / 2; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(group_lane_mask<G>(), hi, o);
+    const float l2 = __shfl_xor_sync(group_lane_mask<G>(), lo, o);
+    add_pair(hi, lo, h2, l2);
+  }
   if constexpr (G > 32) {
-    if ((t & 31) == 0) red[t >> 5] = v;
+    float2 *rf = reinterpret_cast<float2 *>(red);
+    if ((t & 31) == 0) rf[t >> 5] = make_float2(hi, lo);
     group_sync<G>(g);
-    double s = 0.0;
+    hi = 0.f;
+    lo = 0.f;
 #pragma unroll
-    for (int w = 0; w < G / 32; ++w) s += red[w];
+    for (int w = 0; w < G / 32; ++w) add_pair(hi, lo, rf[w].x, rf[w].y);
     group_sync<G>(g);
-    return s;
-  } else {
-    return v;
   }
 }
 
 // Maximum over the group of G threads (same scratch and barriers as
-// group_sum_double).
+// group_sum_pair).
 template <int G> __device__ __forceinline__ float group_max_float(float v, double *red, int g, int t) {
 #pragma unroll
   for (int o = (G < 32 ? G : 32) / 2; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(group_lane_mask<G>(), v, o));
@@ -161,8 +168,25 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
 #pragma unroll
     for (int r = 0; r < 16; ++r) buf[pad16(c * 16 + r)] = v[half * 16 + r];
   }
-  const double ea = ldexp(group_sum_double<G>((double)eah + (double)eal, red, g, t), 2 * xea);
-  const double eb = ldexp(group_sum_double<G>((double)ebh + (double)ebl, red, g, t), 2 * xeb);
+  group_sum_pair<G>(eah, eal, red, g, t);
+  group_sum_pair<G>(ebh, ebl, red, g, t);
+  // FP64 once per group: norms, inverse norms rounded once, and the
+  // spectrum scale factors, handed to the group through `red`
+  if (t == 0) {
+    const double na = sqrt(ldexp((double)eah + (double)eal, 2 * xea));
+    const double nb = sqrt(ldexp((double)ebh + (double)ebl, 2 * xeb));
+    const float ia = na > 0.0 ? (float)(1.0 / na) : 0.f;
+    const float ib = nb > 0.0 ? (float)(1.0 / nb) : 0.f;
+    a.norms[row_a] = na;
+    a.inv_norms[row_a] = ia;
+    if (has_b) {
+      a.norms[row_b] = nb;
+      a.inv_norms[row_b] = ib;
+    }
+    float *scale = reinterpret_cast<float *>(red);
+    scale[0] = a.prescale ? ia : 1.f;
+    scale[1] = a.prescale ? ib : 1.f;
+  }
   group_sync<G>(g);
 
   using PL = FftPlan<P>;
@@ -187,12 +211,7 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
   }
 
   // ---- split the two rows, scale, write packed half spectra
-  const double na = sqrt(ea), nb = sqrt(eb);
-  float sa = 1.f, sb = 1.f;
-  if (a.prescale) {
-    sa = na > 0.0 ? (float)(1.0 / na) : 0.f;
-    sb = nb > 0.0 ? (float)(1.0 / nb) : 0.f;
-  }
+  const float sa = reinterpret_cast<const float *>(red)[0], sb = reinterpret_cast<const float *>(red)[1];
   const long long off_a = row_a * (long long)H, off_b = row_b * (long long)H;
 #pragma unroll 4
   for (int k = t; k < H; k += G) {
@@ -212,14 +231,6 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
     }
     store_spectrum(a.spectra, a.stype, off_a + k, va);
     if (has_b) store_spectrum(a.spectra, a.stype, off_b + k, vb);
-  }
-  if (t == 0) {
-    a.norms[row_a] = na;
-    a.inv_norms[row_a] = na > 0.0 ? (float)(1.0 / na) : 0.f;
-    if (has_b) {
-      a.norms[row_b] = nb;
-      a.inv_norms[row_b] = nb > 0.0 ? (float)(1.0 / nb) : 0.f;
-    }
   }
 }
 
