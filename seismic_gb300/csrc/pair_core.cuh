@@ -221,6 +221,28 @@ __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, 
   }
 }
 
+// Bit q * RL + r set when the thread's last-pass value v[q * RL + r] (output
+// index last_pass_index) lies inside the lag window 1 - shift .. shift (every
+// bit for a window as wide as P).  It depends only on t and shift, so a
+// kernel computes it once and the scan tests one bit per value.
+template <int P> __device__ __forceinline__ uint32_t window_mask(int t, int shift) {
+  using PL = FftPlan<P>;
+  constexpr int RL = PL::R4 ? PL::R4 : (PL::R3 ? PL::R3 : PL::R2);
+  if (2LL * shift >= P) return 0xffffffffu;
+  const int d0 = 1 - shift;
+  const int span = 2 * shift - 1;  // inside iff (m - d0) mod P <= span
+  uint32_t mask = 0;
+#pragma unroll
+  for (int q = 0; q < 32 / RL; ++q) {
+#pragma unroll
+    for (int r = 0; r < RL; ++r) {
+      const int m = last_pass_index<P, RL>(t, q, r);
+      if (((m - d0) & (P - 1)) <= span) mask |= 1u << (q * RL + r);
+    }
+  }
+  return mask;
+}
+
 // Lag-window scan of the two series held in v after the last FFT pass,
 // first-occurrence argmax / argmin, then (thread t == 0 of the group) the
 // epilogue for pairs (ia, ja) (real part) and, if out_b, (ib, jb) (imaginary
@@ -230,28 +252,21 @@ __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, 
 template <int P>
 __device__ __forceinline__ void scan_and_write(const PairArgs &a, float2 (&v)[32], long long ia, long long ja,
                                                long long ib, long long jb, bool out_b, int t, int g, unsigned *red,
-                                               int *hist, bool smem_hist) {
+                                               int *hist, bool smem_hist, uint32_t wmask) {
   using PL = FftPlan<P>;
   constexpr int G = P / 32;
   constexpr int NW = (G + 31) / 32;
   constexpr int RL = PL::R4 ? PL::R4 : (PL::R3 ? PL::R3 : PL::R2);
   const int d0 = 1 - a.shift;
-  const bool full_window = 2LL * a.shift >= P;          // every index m is inside the lag window
-  const int span = full_window ? P : 2 * a.shift - 1;   // inside iff (m - d0) mod P <= span
   const unsigned gmask = group_lane_mask<G>();
 
   // ---- phase A: per-thread max / min of both series.  Values outside the
-  //      lag window are zeroed (0 never wins: only a strictly positive
-  //      maximum / strictly negative minimum counts).
+  //      lag window (wmask = window_mask<P>(t, a.shift)) are zeroed: 0 never
+  //      wins, only a strictly positive maximum / negative minimum counts.
+  if (wmask != 0xffffffffu) {
 #pragma unroll
-  for (int q = 0; q < 32 / RL; ++q) {
-#pragma unroll
-    for (int r = 0; r < RL; ++r) {
-      if (!full_window) {
-        const int m = last_pass_index<P, RL>(t, q, r);
-        if (((m - d0) & (P - 1)) > span) v[q * RL + r] = make_float2(0.f, 0.f);
-      }
-    }
+    for (int e = 0; e < 32; ++e)
+      if (!((wmask >> e) & 1u)) v[e] = make_float2(0.f, 0.f);
   }
   float mx0 = 0.f, mn0 = 0.f, mx1 = 0.f, mn1 = 0.f;
 #pragma unroll

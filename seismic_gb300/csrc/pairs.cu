@@ -99,6 +99,7 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
   // Twiddle roots of the radix-16 passes depend only on the thread: load once.
   TwiddleRoots<P, 1> roots;
   roots.load(t, a.twiddles);
+  const uint32_t wmask = window_mask<P>(t, a.shift);
 
   const int ca = (t == 0) ? 0 : t;
   const int cb = (t == 0) ? S / 2 : S - t;
@@ -153,7 +154,7 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
     float2 v[32];
     assemble_couple(y, t, v);
     inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots);
-    scan_and_write<P>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist);
+    scan_and_write<P>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist, wmask);
   }
 }
 

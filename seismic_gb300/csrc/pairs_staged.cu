@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
     unsigned *red = reds + g * NW * 8;
     TwiddleRoots<P, 1> roots;
     roots.load(t, a.twiddles);
+    const uint32_t wmask = window_mask<P>(t, a.shift);
     const int ca = (t == 0) ? 0 : t;
     const int cb = (t == 0) ? S / 2 : S - t;
     int slot = 0;
@@ -258,7 +259,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
         float2 v[32];
         assemble_couple(y, t, v);
         inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots);
-        scan_and_write<P>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist);
+        scan_and_write<P>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist, wmask);
       }
     }
   }
