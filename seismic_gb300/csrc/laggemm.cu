@@ -942,7 +942,11 @@ cudaError_t launch_lag_rect(const void *cat_ws, long long n_cat, const void *q_w
   LagPlan pl = lag_plan(n_cat, C, length, shift, 0, nhl);
   if (!pl.ok || col_begin < 0 || n_cols < 1 || col_begin + n_cols > n_cat || n_query < 1)
     return cudaErrorInvalidValue;
-  pl.jc = 8;  // queries per item: more items than SMs for a 64-query request
+  pl.jc = 8;  // queries per item: more items than SMs for a 64-query request (4 and 8 measured equal, 16 slower)
+  if (const char *env = getenv("SEISMIC_LAG_RECT_JC")) {  // 1 .. 64, a multiple of jp
+    const int v = atoi(env);
+    if (v >= 1 && v <= 64 && v % pl.jp == 0) pl.jc = v;
+  }
   const size_t cb = lag_plane_bytes(n_cat, C, pl.lp), qb = lag_plane_bytes(n_query, C, pl.lp);
   const char *cw = static_cast<const char *>(cat_ws), *qw = static_cast<const char *>(q_ws);
   LagArgs a{};
