@@ -45,12 +45,22 @@ def build_port() -> str:
     return PORT_SO
 
 
-def build_ref(ref_root: str = "/root/reference") -> str | None:
+def ref_root() -> str | None:
+    """The reference source tree this recipe compiles: $SEISMIC_REF_ROOT, else
+    the read-only checkout at /root/reference; None where neither holds
+    Correlation_in_OMP/correlation_c.cpp (the GPU machine has no reference tree)."""
+    for cand in (os.environ.get("SEISMIC_REF_ROOT"), "/root/reference"):
+        if cand and os.path.exists(os.path.join(cand, "Correlation_in_OMP", "correlation_c.cpp")):
+            return cand
+    return None
+
+
+def build_ref(root: str | None = None) -> str | None:
     """Compile the reference's own OMP source against the shim, if present."""
-    src = os.path.join(ref_root, "Correlation_in_OMP", "correlation_c.cpp")
-    if not os.path.exists(src):
+    root = root or ref_root()
+    if root is None:
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={root}"], check=True)
     return REF_SO
 
 

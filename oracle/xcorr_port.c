@@ -7,7 +7,7 @@
  * Correlation_in_OMP/correlation_c.cpp, kept in the reference's own float
  * operation order so that, built with the same FFT (fftw_shim), it gives
  * bit-identical outputs to the reference source compiled by
- * oracle/build_ref.sh.  Steps and the lines they follow:
+ * the `ref` target of oracle/Makefile.  Steps and the lines they follow:
  *
  *   norms             float sequential sum of squares, sqrt   (:195-204)
  *   forward spectra   r2c of events and of reversed events    (:32-49)

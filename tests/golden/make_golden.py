@@ -66,7 +66,10 @@ CASES = {
 }
 
 
-def main(ref_root: str = "/root/reference") -> None:
+def main(ref_root: str | None = None) -> None:
+    ref_root = ref_root or O.ref_root()
+    if ref_root is None:
+        raise SystemExit("reference tree not found: set SEISMIC_REF_ROOT")
     mod = _load_reference_wrapper(ref_root)
     for name, (build, shift, nthreads, chunk, thr, nh) in CASES.items():
         events = np.ascontiguousarray(build(), dtype=np.float32)

@@ -54,6 +54,35 @@ def test_dropin_cuda_signature_matches_golden(cuda_ok, name):
     check_pairs(got, (g["xcm_pos"], g["xclags_pos"], g["xcm_neg"], g["xclags_neg"]), r, thr, label=name)
 
 
+def test_cuda_dropin_module_as_the_reference_driver_imports_it(cuda_ok, tmp_path):
+    """The CUDA drop-in module run the way Correlation_in_CUDA/test_cuda.py:15,32
+    uses the reference's: ``from correlation_lib import compute_correlation,
+    initialiseRunTime`` with the module's directory on sys.path, in a fresh
+    process, compared with the golden fixture the reference made."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    g = load_golden("family_n48_l1024_s128")
+    np.save(tmp_path / "events.npy", g["events"])
+    script = (
+        "import sys, numpy as np\n"
+        f"sys.path.insert(0, {os.path.join(O.ROOT, 'seismic_gb300', 'cuda')!r})\n"
+        "from correlation_lib import compute_correlation, initialiseRunTime\n"
+        "initialiseRunTime()\n"
+        f"ev = np.load({str(tmp_path / 'events.npy')!r})\n"
+        f"out = compute_correlation(ev, {int(g['shift'])}, 8, {float(g['threshold'])!r})\n"
+        f"np.savez({str(tmp_path / 'out.npz')!r}, *out)\n")
+    subprocess.run([sys.executable, "-c", script], check=True, cwd=str(tmp_path), timeout=300)
+    z = np.load(tmp_path / "out.npz")
+    got = tuple(z[f"arr_{k}"] for k in range(4))
+    ev = g["events"]
+    i, j = O.triu_pairs(ev.shape[0])
+    r = O.fp64_xcorr(ev, int(g["shift"]), i, j, padded=int(g["padded"]))
+    check_pairs(got, (g["xcm_pos"], g["xclags_pos"], g["xcm_neg"], g["xclags_neg"]), r, float(g["threshold"]),
+                label="cuda drop-in module")
+
+
 def test_small_workload_full_triangle_vs_port(cuda_ok):
     """N=200 Ricker events, L=512, lags -511..512, full triangle."""
     ev, shift = synth.make_workload("small")

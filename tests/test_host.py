@@ -2,12 +2,16 @@
 symbol the public header declares, host-only entry points, the Python
 drop-in's padding, and the pair scheduler's coverage of the triangle."""
 import ctypes
+import importlib.util
+import os
 import subprocess
 
 import numpy as np
 import pytest
 
-from seismic_gb300 import _lib, correlation_lib, xcorr
+from seismic_gb300 import _dropin, _lib, xcorr
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_library_exports_every_header_symbol(built_lib):
@@ -54,11 +58,32 @@ def test_dropin_padding_matches_reference_rule():
     evs = np.empty(3, dtype=object)
     for k, length in enumerate((300, 300, 250)):
         evs[k] = Tr(rng.standard_normal(length).astype(np.float32))
-    n, length, p, padded, rev = correlation_lib._pad(evs)
+    n, length, p, padded = _dropin.pad_events(evs)
     assert (n, length, p) == (3, 300, 512)          # L from events[0], P = 1 << L.bit_length()
     np.testing.assert_array_equal(padded[2, :250], evs[2].data)
     assert np.all(padded[2, 250:] == 0)
-    np.testing.assert_array_equal(rev[0, :300], evs[0].data[::-1])
+    # a plain (N, L) array takes the vectorised path, same result
+    plain = rng.standard_normal((4, 100)).astype(np.float32)
+    n, length, p, padded = _dropin.pad_events(plain)
+    assert (n, length, p) == (4, 100, 128)
+    np.testing.assert_array_equal(padded[:, :100], plain)
+    assert np.all(padded[:, 100:] == 0)
+
+
+def test_cuda_dropin_imports_under_the_reference_module_name():
+    """Correlation_in_CUDA/test_cuda.py:15 does ``from correlation_lib import
+    compute_correlation, initialiseRunTime``: the CUDA drop-in must import
+    under that name with its directory on sys.path, with the reference's
+    signatures (Correlation_in_CUDA/correlation_lib.py:31,101)."""
+    import inspect
+    spec = importlib.util.spec_from_file_location(
+        "correlation_lib", os.path.join(ROOT, "seismic_gb300", "cuda", "correlation_lib.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    assert list(inspect.signature(mod.compute_correlation).parameters) == ["events", "shift", "num_threads",
+                                                                            "threshold"]
+    assert list(inspect.signature(mod.initialiseRunTime).parameters) == []
+    assert callable(mod.initialise_library)
 
 
 def test_packed_index():

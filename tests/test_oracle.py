@@ -43,8 +43,7 @@ def test_golden_against_fp64(name):
     assert ag.lag_mismatch <= near, ag
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/Correlation_in_OMP/correlation_c.cpp"),
-                    reason="reference tree not present")
+@pytest.mark.skipif(O.ref_root() is None, reason="reference tree not present (set SEISMIC_REF_ROOT)")
 def test_port_matches_reference_build_random():
     ev = synth.family_catalog(33, 1, 700, n_families=3, seed=77)[:, 0]
     a = O.port_correlation_cpp(ev, 300, 0.1, 9)
