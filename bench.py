@@ -405,7 +405,7 @@ def run_ours(args):
 
     d_ev = torch.from_numpy(ev).to(dev)
     spectra = torch.empty(rows * (p // 2) * 2, dtype=torch.float32, device=dev)
-    norms = torch.empty(rows + (rows + 1) // 2, dtype=torch.float64, device=dev)  # FP64 norms + FP32 inverses
+    norms = torch.empty(2 * rows, dtype=torch.float64, device=dev)  # FP64 norms + FP64 inverse norms
     vp = torch.empty(npairs, dtype=torch.float32, device=dev)
     lp = torch.empty(npairs, dtype=torch.int32, device=dev)
     vn = torch.empty(npairs, dtype=torch.float32, device=dev)

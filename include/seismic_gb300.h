@@ -123,7 +123,8 @@ size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int eve
 
 /* Returns SEISMIC_OK, or SEISMIC_ERR_DEVICE_TIMEOUT if a kernel of this
  * library gave up a bounded wait since the last check (and clears the flag).
- * Synchronises the current device. */
+ * Synchronises the current device.  Allocates nothing (no stream, no
+ * buffer), so callers of seismic_xcorr_device_noalloc may use it. */
 int seismic_check_device_error(void);
 
 /* All-pairs correlation of device-resident events.
@@ -156,9 +157,8 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
 /* Kernel (a) alone: packed half spectra and FP64 norms of every (event,
  * channel) row.  d_spectra: n_events*n_channels rows of padded_size/2
  * float2 (slot 0 = (Re X[0], Re X[P/2]), slot k = X[k]); d_norms: room for
- * rows = n_events*n_channels doubles (the norms) followed by rows floats
- * (1/norm computed in FP64 and rounded once, 0 for a zero row): 12*rows
- * bytes.  prescale != 0 scales each row by 1/norm (0 for a zero row), the
+ * rows = n_events*n_channels doubles (the norms) followed by rows doubles
+ * (1/norm, 0 for a zero row): 16*rows bytes.  prescale != 0 scales each row by 1/norm (0 for a zero row), the
  * form the multichannel mean uses. */
 int seismic_spectra_device(const float *d_events, long long n_events, int n_channels, int event_length,
                            long long event_stride, long long channel_stride, int padded_size, int prescale,
@@ -196,12 +196,16 @@ long long seismic_pair_couples(long long n_events, int padded_size, int n_channe
  * the spectra and norms is one fixed array of seismic_noalloc_scratch_bytes()
  * (64 MiB) inside this library, reserved on every device that uses it until
  * the process exits.  Catalogs needing more than that
- * (n_events*n_channels*(padded_size*4 + 12) bytes, 256-byte rounded per part)
+ * (n_events*n_channels*(padded_size*4 + 16) bytes, 256-byte rounded per part)
  * are rejected with SEISMIC_ERR_WORKSPACE_TOO_SMALL.  The first call on a
  * device sets that device up, so make it before any stream capture.  All
  * calls share the scratch: calls that overlap on the GPU (other streams or
  * threads) race and must be serialised by the caller.  The call allocates
- * nothing: no cudaMalloc, no cudaFree, no allocating library routine. */
+ * nothing: no cudaMalloc, no cudaFree, no allocating library routine.  It
+ * returns once the kernels are queued; a kernel whose bounded wait ran out
+ * leaves the device error flag set, which seismic_check_device_error()
+ * (allocation-free as well) reads and clears after the caller has
+ * synchronised. */
 int seismic_xcorr_device_noalloc(const float *d_events, long long n_events, int n_channels, int event_length,
                                  long long event_stride, long long channel_stride, int padded_size, int shift,
                                  float threshold, int n_classes_hist, float *d_vals_pos, int *d_lags_pos,

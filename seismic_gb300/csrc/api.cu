@@ -10,6 +10,7 @@
 //   D2H of the four packed outputs and the histograms.
 #include <atomic>
 #include <cstdarg>
+#include <map>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -225,16 +226,44 @@ cudaError_t launch_pair_work(int P, const PairArgs &a, int sm_count, int ctas_pe
   if (staged_supported(P, a)) return launch_pairs_staged(P, a, sm_count, stream);
   PairArgs d = a;  // direct form: L2 row bands of tiles (triangle mode)
   if (!d.rect && d.band_tiles == 0) d.band_tiles = l2_band_tiles(d.n_channels, P, d.stype ? 4 : 8, d.tile);
-  static int ctas_cache[16] = {0};
-  const int lp2 = 31 - __builtin_clz((unsigned)P);
-  if (!ctas_cache[lp2]) ctas_cache[lp2] = pair_ctas_per_sm(P);
-  const int ctas = (ctas_per_sm > 0 && ctas_per_sm < ctas_cache[lp2]) ? ctas_per_sm : ctas_cache[lp2];
+  const int occ = pair_ctas_per_sm_cached(P);
+  const int ctas = (ctas_per_sm > 0 && ctas_per_sm < occ) ? ctas_per_sm : occ;
   const int NG = groups_per_cta(P);
   long long want = (d.couple_end - d.couple_begin + NG - 1) / NG;
   long long grid = (long long)sm_count * ctas;
   if (want < grid) grid = want;
   if (grid < 1) grid = 1;
   return launch_pairs(P, d, (int)grid, stream);
+}
+
+cudaError_t ensure_dynamic_smem(const void *func, int bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  static std::mutex m;
+  static std::map<std::pair<const void *, int>, int> done;  // (kernel, device) -> bytes set
+  std::lock_guard<std::mutex> lock(m);
+  auto it = done.find({func, dev});
+  if (it != done.end() && it->second >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done[{func, dev}] = bytes;
+  return e;
+}
+
+int pair_ctas_per_sm_cached(int P) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+  static std::mutex m;
+  static std::map<std::pair<int, int>, int> cache;  // (device, P) -> CTAs per SM
+  {
+    std::lock_guard<std::mutex> lock(m);
+    auto it = cache.find({dev, P});
+    if (it != cache.end()) return it->second;
+  }
+  const int n = pair_ctas_per_sm(P);  // sets the kernel attribute on this device
+  std::lock_guard<std::mutex> lock(m);
+  cache[{dev, P}] = n;
+  return n;
 }
 
 // Row bands of the pair form launch_pair_work runs on the triangle of these
@@ -360,17 +389,17 @@ size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int eve
 }
 
 int seismic_check_device_error(void) {
+  // Allocation-free (usable by callers of seismic_xcorr_device_noalloc): no
+  // stream, no buffer, only the flag's symbol address and two small copies.
   set_status(SEISMIC_OK, "");
-  int dev;
-  DeviceState *st;
-  int s = ensure_device(&dev, &st);
-  if (s) return s;
+  int *flag_addr = device_error_flag();
+  if (!flag_addr) return set_status(SEISMIC_ERR_CUDA, "device error flag address");
   SEISMIC_TRY(cudaDeviceSynchronize(), "device synchronise");
   int flag = 0;
-  SEISMIC_TRY(cudaMemcpy(&flag, st->error_flag, sizeof(int), cudaMemcpyDeviceToHost), "error flag read");
+  SEISMIC_TRY(cudaMemcpy(&flag, flag_addr, sizeof(int), cudaMemcpyDeviceToHost), "error flag read");
   if (flag) {
     const int zero = 0;
-    SEISMIC_TRY(cudaMemcpy(st->error_flag, &zero, sizeof(int), cudaMemcpyHostToDevice), "error flag clear");
+    SEISMIC_TRY(cudaMemcpy(flag_addr, &zero, sizeof(int), cudaMemcpyHostToDevice), "error flag clear");
     return set_status(SEISMIC_ERR_DEVICE_TIMEOUT, "a kernel gave up a bounded wait; its results are invalid");
   }
   return SEISMIC_OK;

@@ -27,25 +27,24 @@ struct SpectraArgs {
   int stype;               // spectrum storage: 0 float2, 1 half2 (FP16), 2 bfloat162 (BF16)
   void *spectra;           // out [n_events*n_channels][P/2] of stype
   double *norms;           // out [n_events*n_channels], FP64 L2 norms
-  float *inv_norms;        // out [n_events*n_channels], 1/norm computed in FP64, rounded once (0 for 0)
+  double *inv_norms;       // out [n_events*n_channels], FP64 1/norm (0 for 0)
   const float2 *twiddles;  // twiddle_table()
 };
 
-// A norms buffer holds `rows` FP64 norms followed by `rows` FP32 inverse norms.
-inline size_t norms_buffer_bytes(long long rows) { return ((size_t)rows * 12 + 255) / 256 * 256; }
-__host__ __device__ inline float *inverse_norms_of(double *norms, long long rows) {
-  return reinterpret_cast<float *>(norms + rows);
-}
-__host__ __device__ inline const float *inverse_norms_of(const double *norms, long long rows) {
-  return reinterpret_cast<const float *>(norms + rows);
+// A norms buffer holds `rows` FP64 norms followed by `rows` FP64 inverse
+// norms: the final coefficient normalisation of every form is FP64.
+inline size_t norms_buffer_bytes(long long rows) { return ((size_t)rows * 16 + 255) / 256 * 256; }
+__host__ __device__ inline double *inverse_norms_of(double *norms, long long rows) { return norms + rows; }
+__host__ __device__ inline const double *inverse_norms_of(const double *norms, long long rows) {
+  return norms + rows;
 }
 
 struct PairArgs {
   const void *spectra;     // [n_events*n_channels][P/2] of stype
   int stype;               // 0 float2, 1 half2, 2 bfloat162
   const double *norms;     // [n_events*n_channels]
-  const float *inv_norms;  // [n_events*n_channels], see SpectraArgs
-  const float *inv_norms_q;  // rectangle mode: the queries' inverse norms
+  const double *inv_norms;    // [n_events*n_channels], see SpectraArgs
+  const double *inv_norms_q;  // rectangle mode: the queries' inverse norms
   long long n_events;
   int n_channels;
   int shift;               // lags d = 1-shift .. shift
@@ -207,6 +206,16 @@ cudaError_t launch_lag_rect(const void *cat_ws, long long n_cat, const void *q_w
                             float *vp, int *lp, float *vn, int *ln, int *error_flag, int sm_count, cudaStream_t s);
 // Device address of the kernels' error flag (set when a bounded wait runs out).
 int *device_error_flag();
+
+// Raises the dynamic shared-memory limit of kernel `func` to at least `bytes`
+// on the CURRENT device.  The attribute is per device context, so the
+// setting is remembered per (kernel, device) under a lock: a second GPU in
+// the same process gets its own cudaFuncSetAttribute.  Not a stream
+// operation; the first call for a device should come before any capture.
+cudaError_t ensure_dynamic_smem(const void *func, int bytes);
+// Occupancy of the direct pair form at size P on the current device, cached
+// per device (api.cu).
+int pair_ctas_per_sm_cached(int P);
 
 // Status plumbing shared by the entry points of every translation unit
 // (defined in api.cu): set the calling thread's status / message.

@@ -111,7 +111,7 @@ __global__ void lag_prep_kernel(const float *__restrict__ ev, long long n, int C
   }
   if (lane == 0) {
     norms[row] = nrm;
-    inverse_norms_of(norms, n * C)[row] = nrm > 0.0 ? (float)(1.0 / nrm) : 0.f;
+    inverse_norms_of(norms, n * C)[row] = nrm > 0.0 ? 1.0 / nrm : 0.0;
   }
 }
 
@@ -660,24 +660,24 @@ __global__ void __launch_bounds__(kLagThreads, 1)
           if (p < njp && (RECT ? (i < a.col_begin + a.n_cols && i < N) : (i < N && j >= i))) {
             const float best = bestp[p], worst = worstp[p];
             const int bn = bnp[p], wn = wnp[p];
-            // per-event 1/norm factors come from FP64 (prep kernel); per pair FP32
-            const float *inv = inverse_norms_of(a.norms, N * C);  // A side
-            const float *inv_j = RECT ? inverse_norms_of(a.q_norms, a.n_query * C) : inv;
-            float scale;
+            // final normalisation in FP64: per-event FP64 1/norm (prep kernel)
+            const double *inv = inverse_norms_of(a.norms, N * C);  // A side
+            const double *inv_j = RECT ? inverse_norms_of(a.q_norms, a.n_query * C) : inv;
+            double scale;
             bool live = false;
             if (a.prescaled) {
-              for (int cc = 0; cc < C; ++cc) live |= (inv[i * C + cc] > 0.f) && (inv_j[j * C + cc] > 0.f);
-              scale = 1.0f / (float)C;
+              for (int cc = 0; cc < C; ++cc) live |= (inv[i * C + cc] > 0.0) && (inv_j[j * C + cc] > 0.0);
+              scale = 1.0 / (double)C;
             } else {
-              const float ni = inv[i * C], nj = inv_j[j * C];
-              live = ni > 0.f && nj > 0.f;
+              const double ni = inv[i * C], nj = inv_j[j * C];
+              live = ni > 0.0 && nj > 0.0;
               scale = ni * nj;
             }
             float vp = 0.f, vn = 0.f;
             int lp = 0, ln = 0;
             if (live) {
-              vp = best * scale;
-              vn = worst * scale;
+              vp = (float)((double)best * scale);
+              vn = (float)((double)worst * scale);
               const int lag0 = RECT ? 1 - a.shift : a.shift;  // lag at n = 0
               const int dir = RECT ? 1 : -1;                  // lag step per n
               lp = best > 0.f ? lag0 + dir * bn : 0;
@@ -866,12 +866,9 @@ static cudaError_t launch_lag_kernel(LagArgs &a, const LagPlan &pl, const unsign
   void (*kern)(const CUtensorMap, const CUtensorMap, LagArgs) =
       a.nhl == 1 ? (a.rect ? lag_gemm_kernel<1, true> : lag_gemm_kernel<1, false>)
                  : (a.rect ? lag_gemm_kernel<2, true> : lag_gemm_kernel<2, false>);
-  static bool configured[4] = {false, false, false, false};
-  const int kid = (a.nhl == 1 ? 0 : 2) + (a.rect ? 1 : 0);
-  if (!configured[kid]) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+  {
+    cudaError_t e = ensure_dynamic_smem((const void *)kern, 227 * 1024);
     if (e != cudaSuccess) return e;
-    configured[kid] = true;
   }
   if (items <= 0) return cudaSuccess;
   const long long grid = items < sm_count ? items : sm_count;

@@ -24,6 +24,12 @@
 //    Serialise them, e.g. on one stream.
 //  * Catalogs whose spectra + norms exceed the scratch are rejected with
 //    SEISMIC_ERR_WORKSPACE_TOO_SMALL before anything is launched.
+//  * The call returns once the kernels are queued.  A kernel whose bounded
+//    wait ran out leaves the device error flag set (its outputs are then
+//    invalid); after synchronising the stream, seismic_check_device_error()
+//    reads and clears that flag, and it allocates nothing either.
+//  * Launch shapes come from the same autotuner cache as seismic_xcorr_device
+//    (a host-side lookup), so both entry points run the same kernels.
 #include <cstdio>
 #include <mutex>
 
@@ -106,11 +112,11 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
 
   const long long rows = n_events * n_channels;
   const size_t spec_b = round256((size_t)rows * (size_t)(padded_size / 2) * sizeof(float2));
-  const size_t norm_b = norms_buffer_bytes(rows);  // FP64 norms + FP32 inverse norms
+  const size_t norm_b = norms_buffer_bytes(rows);  // FP64 norms + FP64 inverse norms
   if (spec_b + norm_b > kNoAllocScratchBytes) {
     char msg[200];
     snprintf(msg, sizeof(msg),
-             "catalog needs %zu bytes of scratch (n_events*n_channels*(padded_size*4 + 12)); "
+             "catalog needs %zu bytes of scratch (n_events*n_channels*(padded_size*4 + 16)); "
              "the no-alloc entry point has %zu",
              spec_b + norm_b, kNoAllocScratchBytes);
     return report_status(SEISMIC_ERR_WORKSPACE_TOO_SMALL, msg);
@@ -158,12 +164,13 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   pa.lags_neg = d_lags_neg;
   pa.max_hist = d_max_hist;
   pa.min_hist = d_min_hist;
-  pa.tile = pair_tile_for(padded_size);
+  const TuneEntry tune = tune_lookup(padded_size, n_channels);  // host-side cache, as seismic_xcorr_device
+  pa.tile = tune.tile;
   pa.twiddles = d->twiddles;
   pa.error_flag = d->error_flag;
   pa.couple_begin = 0;
   pa.couple_end = pair_work_total(padded_size, pa);
-  e = launch_pair_work(padded_size, pa, d->sm_count, 0, st);
+  e = launch_pair_work(padded_size, pa, d->sm_count, tune.ctas_per_sm, st);
   if (e != cudaSuccess) return report_cuda(e, "pair kernel launch");
   note_launches(1);
   return SEISMIC_OK;

@@ -335,34 +335,34 @@ __device__ __forceinline__ void scan_and_write(const PairArgs &a, float2 (&v)[32
   }
 
   // ---- epilogue: normalise, histogram, threshold, packed write.  The
-  //      per-event factors 1/norm were computed in FP64 by the spectra
-  //      kernel and rounded once; the per-pair scaling is FP32 (<= 4 ulp),
-  //      which keeps the slow FP64 pipe out of the pair loop.
+  //      final normalisation is FP64: the per-event FP64 inverse norms of the
+  //      spectra kernel, the 1/P of the unnormalised inverse FFT (and 1/C of
+  //      the channel mean), one product per pair by one thread of the group.
   if (t == 0) {
     const long long N = a.n_events;
     const int C = a.n_channels;
-    const float *inv_i = a.rect ? a.inv_norms_q : a.inv_norms;
+    const double *inv_i = a.rect ? a.inv_norms_q : a.inv_norms;
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
       if (p == 1 && !out_b) break;
       const long long i = p == 0 ? ia : ib;
       const long long j = p == 0 ? ja : jb;
       const unsigned kp = key[2 * p], kn = key[2 * p + 1];
-      float scale;
+      double scale;
       bool live = false;
       if (a.prescaled) {  // spectra already carry 1/norm: mean over channels
-        for (int c = 0; c < C; ++c) live |= (inv_i[i * C + c] > 0.f) && (a.inv_norms[j * C + c] > 0.f);
-        scale = 1.0f / ((float)P * (float)C);
+        for (int c = 0; c < C; ++c) live |= (inv_i[i * C + c] > 0.0) && (a.inv_norms[j * C + c] > 0.0);
+        scale = 1.0 / ((double)P * (double)C);
       } else {
-        const float ni = inv_i[i * C], nj = a.inv_norms[j * C];
-        live = ni > 0.f && nj > 0.f;
-        scale = (ni * nj) * (1.0f / (float)P);
+        const double ni = inv_i[i * C], nj = a.inv_norms[j * C];
+        live = ni > 0.0 && nj > 0.0;
+        scale = (ni * nj) * (1.0 / (double)P);
       }
       float vp = 0.f, vn = 0.f;
       int lp = 0, ln = 0;
       if (live) {
-        vp = __uint_as_float(kp) * scale;
-        vn = -(__uint_as_float(kn) * scale);
+        vp = (float)((double)__uint_as_float(kp) * scale);
+        vn = (float)(-((double)__uint_as_float(kn) * scale));
         lp = kp ? lag[2 * p] : 0;
         ln = kn ? lag[2 * p + 1] : 0;
         if (a.n_hist > 0) {

@@ -219,8 +219,7 @@ template <int P> static size_t batched_pair_smem_t(int max_hist) {
 
 template <int P> static int batched_ctas_t(int max_hist) {
   int n = 0;
-  cudaFuncSetAttribute(batched_pair_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)batched_pair_smem_t<P>(kSmemHistMax));
+  ensure_dynamic_smem((const void *)batched_pair_kernel<P>, (int)batched_pair_smem_t<P>(kSmemHistMax));
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batched_pair_kernel<P>, 256,
                                                     batched_pair_smem_t<P>(max_hist)) != cudaSuccess)
     n = 1;
@@ -280,13 +279,8 @@ template <int P, int ST> static cudaError_t launch_pairs_st(const PairArgs &a, i
   constexpr int G = P / 32;
   constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
   const size_t smem = pair_smem_bytes<P>(a.n_hist);
-  static int configured_bytes = 0;
-  if ((int)smem > configured_bytes) {
-    const int want = (int)pair_smem_bytes<P>(kSmemHistMax);
-    cudaError_t e = cudaFuncSetAttribute(pair_kernel<P, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
-    if (e != cudaSuccess) return e;
-    configured_bytes = want;
-  }
+  cudaError_t e = ensure_dynamic_smem((const void *)pair_kernel<P, ST>, (int)pair_smem_bytes<P>(kSmemHistMax));
+  if (e != cudaSuccess) return e;
   if (a.couple_end <= a.couple_begin) return cudaSuccess;
   pair_kernel<P, ST><<<grid, NG * G, smem, s>>>(a);
   return cudaGetLastError();
@@ -306,8 +300,7 @@ template <int P> static int ctas_per_sm_t() {
   const size_t smem = pair_smem_bytes<P>(64);
   constexpr int G = P / 32;
   constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
-  cudaFuncSetAttribute(pair_kernel<P, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)pair_smem_bytes<P>(kSmemHistMax));
+  ensure_dynamic_smem((const void *)pair_kernel<P, 0>, (int)pair_smem_bytes<P>(kSmemHistMax));
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_kernel<P, 0>, NG * G, smem) != cudaSuccess) n = 1;
   return n > 0 ? n : 1;
 }

@@ -339,12 +339,9 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
   a.ring = K;
   const size_t hist_bytes = (a.n_hist > 0 && a.n_hist <= kStagedHistMax) ? (size_t)2 * a.n_hist * sizeof(int) : 0;
   const size_t smem = SH::RING_OFF + (size_t)K * unit + (size_t)2 * K * sizeof(uint64_t) + hist_bytes;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(staged_pair_kernel<P, NWARP, RU, ST>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kStagedSmemBudget);
+  {
+    cudaError_t e = ensure_dynamic_smem((const void *)staged_pair_kernel<P, NWARP, RU, ST>, (int)kStagedSmemBudget);
     if (e != cudaSuccess) return e;
-    configured = true;
   }
   a.band_tiles = l2_band_tiles(a.n_channels, P, (int)sizeof(ST_T), SH::T);
 

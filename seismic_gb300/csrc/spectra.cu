@@ -175,8 +175,8 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
   if (t == 0) {
     const double na = sqrt(ldexp((double)eah + (double)eal, 2 * xea));
     const double nb = sqrt(ldexp((double)ebh + (double)ebl, 2 * xeb));
-    const float ia = na > 0.0 ? (float)(1.0 / na) : 0.f;
-    const float ib = nb > 0.0 ? (float)(1.0 / nb) : 0.f;
+    const double ia = na > 0.0 ? 1.0 / na : 0.0;
+    const double ib = nb > 0.0 ? 1.0 / nb : 0.0;
     a.norms[row_a] = na;
     a.inv_norms[row_a] = ia;
     if (has_b) {
@@ -184,8 +184,8 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
       a.inv_norms[row_b] = ib;
     }
     float *scale = reinterpret_cast<float *>(red);
-    scale[0] = a.prescale ? ia : 1.f;
-    scale[1] = a.prescale ? ib : 1.f;
+    scale[0] = a.prescale ? (float)ia : 1.f;
+    scale[1] = a.prescale ? (float)ib : 1.f;
   }
   group_sync<G>(g);
 
@@ -243,12 +243,8 @@ template <int P> static cudaError_t launch_spectra_t(const SpectraArgs &a, cudaS
   if (ctas <= 0) return cudaSuccess;
   if (ctas > 0x7fffffffLL) return cudaErrorInvalidValue;
   const size_t smem = (size_t)NG * padded_len<P>() * sizeof(float2) + (size_t)NG * 2 * ((G + 31) / 32) * sizeof(double);
-  static bool configured = false;  // benign race: idempotent attribute set
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(spectra_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  cudaError_t e = ensure_dynamic_smem((const void *)spectra_kernel<P>, (int)smem);
+  if (e != cudaSuccess) return e;
   spectra_kernel<P><<<(unsigned)ctas, NG * G, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -285,13 +281,9 @@ cudaError_t launch_batched_spectra(const BatchCatalog *cats, const BatchItem *it
                                    cudaStream_t s) {
   // every size uses NG * (P + P/16) float2 = 69,632 bytes plus <= 2 KB of reduction slots
   const size_t smem = (size_t)8 * (8192 + 512) + 2048;
-  static bool configured = false;  // first call happens before any capture (batch planning)
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(batched_spectra_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  // the first call per device happens before any capture (batch planning)
+  cudaError_t e = ensure_dynamic_smem((const void *)batched_spectra_kernel, (int)smem);
+  if (e != cudaSuccess) return e;
   if (n_items <= 0) return cudaSuccess;
   batched_spectra_kernel<<<grid, 256, smem, s>>>(cats, items, n_items);
   return cudaGetLastError();

@@ -190,7 +190,7 @@ def test_pair_ranges_on_streams_compose_the_triangle(cuda_ok, n, length, shift):
     t = torch.from_numpy(ev).cuda()
     rows = n * c
     spec = torch.empty(rows * p // 2 * 2, device="cuda")
-    norms = torch.empty(rows + (rows + 1) // 2, dtype=torch.float64, device="cuda")
+    norms = torch.empty(2 * rows, dtype=torch.float64, device="cuda")
     _lib.check(lib.seismic_spectra_device(t.data_ptr(), n, c, length, c * length, length, p, 1, spec.data_ptr(),
                                           norms.data_ptr(), None))
     m = n * (n + 1) // 2
@@ -288,7 +288,7 @@ def test_spectra_norms_fp64_over_amplitude_range(cuda_ok, length):
     p = xcorr.resolve_padded_size(length, length)
     t = torch.from_numpy(ev).cuda()
     spec = torch.empty(n * p // 2 * 2, device="cuda")
-    norms = torch.empty(n + (n + 1) // 2, dtype=torch.float64, device="cuda")
+    norms = torch.empty(2 * n, dtype=torch.float64, device="cuda")
     _lib.check(lib.seismic_spectra_device(t.data_ptr(), n, 1, length, length, length, p, 0, spec.data_ptr(),
                                           norms.data_ptr(), None))
     torch.cuda.synchronize()

@@ -50,6 +50,9 @@ def test_noalloc_matches_regular_entry_point_twice(cuda_ok):
     cases = [
         (synth.family_catalog(96, 3, 1000, n_families=4, seed=301), 1000, 0.1, 12),
         (synth.ricker_catalog(150, 512, seed=302), 512, 0.0, 20),
+        # padded size 256: the direct-load pair form, whose row bands are
+        # planned inside the launch, through the same fixed scratch
+        (synth.family_catalog(70, 1, 200, n_families=3, seed=303), 50, 0.0, 10),
     ]
     for ev, shift, thr, nh in cases:
         t_ev = torch.from_numpy(ev).cuda()
@@ -64,12 +67,35 @@ def test_noalloc_matches_regular_entry_point_twice(cuda_ok):
         assert not np.any(got[1] == -2**31) and not np.any(got[3] == -2**31)
 
 
+def test_noalloc_accepts_catalog_filling_the_scratch_exactly(cuda_ok):
+    """One channel at padded size 4096: 16 KiB of spectra + 16 B of FP64 norm
+    and inverse norm per event, each part rounded up to 256 B.  4092 events
+    need 4092*16384 + 65536 bytes = exactly 64 MiB: accepted, same results
+    as the regular entry point, and the check call reports no timeout."""
+    import torch
+    lib = cuda_ok
+    cap = lib.seismic_noalloc_scratch_bytes()
+    n = 4092
+    assert n * 16384 + ((16 * n + 255) // 256) * 256 == cap
+    ev = synth.family_catalog(n, 1, 2048, n_families=16, seed=304)
+    t_ev = torch.from_numpy(ev).cuda()
+    stream = torch.cuda.Stream()
+    got, got_h = _run(lib, "seismic_xcorr_device_noalloc", t_ev, 2048, 0.0, 20, stream)
+    assert lib.seismic_check_device_error() == 0
+    exp, exp_h = _run(lib, "seismic_xcorr_device", t_ev, 2048, 0.0, 20, stream)
+    assert np.abs(got[0] - exp[0]).max() <= COEF_TOL
+    assert np.abs(got[2] - exp[2]).max() <= COEF_TOL
+    np.testing.assert_array_equal(got[1], exp[1])
+    np.testing.assert_array_equal(got[3], exp[3])
+    np.testing.assert_array_equal(got_h, exp_h)
+
+
 def test_noalloc_rejects_catalog_beyond_scratch(cuda_ok):
     import torch
     lib = cuda_ok
     cap = lib.seismic_noalloc_scratch_bytes()
     assert cap == 64 << 20
-    n = cap // (4096 * 4) + 1           # one channel at padded size 4096 needs 16 KiB per event
+    n = 4093                            # one event more than fills the scratch exactly
     m = n * (n + 1) // 2
     ev = torch.zeros(n, 2048, device="cuda")       # real buffers of the full size
     outs = [torch.zeros(m, device="cuda"), torch.zeros(m, dtype=torch.int32, device="cuda"),
