@@ -787,7 +787,7 @@ def run_serving(args):
     # station subset of 1,000..50,000
     levels = []
     for rate in (100, 300, 1000):
-        n_req = min(48, int(rate * 1.0))
+        n_req = {100: 200, 300: 300, 1000: 200}[rate]  # 2 s, 1 s and 0.2 s of offered load
         gaps = rng.exponential(1.0 / rate, size=n_req)
         reqs = []
         for k in range(n_req):

@@ -157,8 +157,9 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
 /* Kernel (a) alone: packed half spectra and FP64 norms of every (event,
  * channel) row.  d_spectra: n_events*n_channels rows of padded_size/2
  * float2 (slot 0 = (Re X[0], Re X[P/2]), slot k = X[k]); d_norms: room for
- * rows = n_events*n_channels doubles (the norms) followed by rows doubles
- * (1/norm, 0 for a zero row): 16*rows bytes.  prescale != 0 scales each row by 1/norm (0 for a zero row), the
+ * rows = n_events*n_channels doubles (the norms) followed by rows float
+ * pairs (1/norm computed in FP64, kept as hi + lo floats; 0 for a zero
+ * row): 16*rows bytes.  prescale != 0 scales each row by 1/norm (0 for a zero row), the
  * form the multichannel mean uses. */
 int seismic_spectra_device(const float *d_events, long long n_events, int n_channels, int event_length,
                            long long event_stride, long long channel_stride, int padded_size, int prescale,

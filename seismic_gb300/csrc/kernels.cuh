@@ -27,24 +27,35 @@ struct SpectraArgs {
   int stype;               // spectrum storage: 0 float2, 1 half2 (FP16), 2 bfloat162 (BF16)
   void *spectra;           // out [n_events*n_channels][P/2] of stype
   double *norms;           // out [n_events*n_channels], FP64 L2 norms
-  double *inv_norms;       // out [n_events*n_channels], FP64 1/norm (0 for 0)
+  float2 *inv_norms;       // out [n_events*n_channels], FP64 1/norm as hi + lo floats (0 for 0)
   const float2 *twiddles;  // twiddle_table()
 };
 
-// A norms buffer holds `rows` FP64 norms followed by `rows` FP64 inverse
-// norms: the final coefficient normalisation of every form is FP64.
+// A norms buffer holds `rows` FP64 norms followed by `rows` inverse norms
+// 1/norm, each computed in FP64 and stored as an unevaluated float pair
+// hi + lo (hi = the float nearest to it, lo = the float nearest to the
+// rest): 48 significant bits, from which the final normalisation of every
+// form is computed at FP64-equivalent accuracy without FP64 instructions in
+// the FFT pair loop (compensated_scale below).
 inline size_t norms_buffer_bytes(long long rows) { return ((size_t)rows * 16 + 255) / 256 * 256; }
-__host__ __device__ inline double *inverse_norms_of(double *norms, long long rows) { return norms + rows; }
-__host__ __device__ inline const double *inverse_norms_of(const double *norms, long long rows) {
-  return norms + rows;
+__host__ __device__ inline float2 *inverse_norms_of(double *norms, long long rows) {
+  return reinterpret_cast<float2 *>(norms + rows);
+}
+__host__ __device__ inline const float2 *inverse_norms_of(const double *norms, long long rows) {
+  return reinterpret_cast<const float2 *>(norms + rows);
+}
+// FP64 value -> (hi, lo) float pair.
+__host__ __device__ inline float2 split_double(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
 }
 
 struct PairArgs {
   const void *spectra;     // [n_events*n_channels][P/2] of stype
   int stype;               // 0 float2, 1 half2, 2 bfloat162
   const double *norms;     // [n_events*n_channels]
-  const double *inv_norms;    // [n_events*n_channels], see SpectraArgs
-  const double *inv_norms_q;  // rectangle mode: the queries' inverse norms
+  const float2 *inv_norms;    // [n_events*n_channels], see SpectraArgs
+  const float2 *inv_norms_q;  // rectangle mode: the queries' inverse norms
   long long n_events;
   int n_channels;
   int shift;               // lags d = 1-shift .. shift
@@ -81,7 +92,20 @@ struct PairArgs {
   int band_tiles;
   int ring;
   int *error_flag;
+  // Poll limit of the staged form's producer waits (0: the built-in limit,
+  // seconds of back-off).  Set from SEISMIC_DEVICE_WAIT_POLLS: a few polls
+  // make the waits run out on a healthy GPU, which is how the abort path and
+  // its error status are tested.
+  unsigned wait_limit;
 };
+
+// SEISMIC_DEVICE_WAIT_POLLS (1 .. 2^30), else 0.
+inline unsigned device_wait_polls() {
+  const char *e = getenv("SEISMIC_DEVICE_WAIT_POLLS");
+  if (!e) return 0;
+  const long long v = atoll(e);
+  return (v >= 1 && v <= (1LL << 30)) ? (unsigned)v : 0u;
+}
 
 // Tile rows per L2 band of the triangle walk (PairArgs::band_tiles) so
 // that the spectra of one band's events take about 48 MB of L2

@@ -111,7 +111,7 @@ __global__ void lag_prep_kernel(const float *__restrict__ ev, long long n, int C
   }
   if (lane == 0) {
     norms[row] = nrm;
-    inverse_norms_of(norms, n * C)[row] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    inverse_norms_of(norms, n * C)[row] = split_double(nrm > 0.0 ? 1.0 / nrm : 0.0);
   }
 }
 
@@ -155,6 +155,7 @@ struct LagArgs {
   int nhl;
   int kgroup;     // K-chunks per MMA group (1 .. kLagGroupMax, at most stages / 2)
   long long blk_begin, blk_end;  // triangle: the 128-event blocks this launch walks
+  unsigned wait_limit;  // polls of each bounded wait (0: kLagWaitPolls); SEISMIC_DEVICE_WAIT_POLLS
 };
 
 struct LagSmem {  // offsets into dynamic shared memory (base 1024-aligned)
@@ -181,8 +182,14 @@ static LagSmem lag_smem_layout(const LagArgs &a) {
   return s;
 }
 
+// Default poll limit of the lag-GEMM's waits (with back-off: about 2 s).
+constexpr uint32_t kLagWaitPolls = 1u << 22;
+
+// Bounded wait.  The CTA's poll limit (LagArgs::wait_limit, or the default)
+// is the shared word right after its abort flag.
 __device__ __forceinline__ bool lag_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err) {
-  for (uint32_t it = 0; it < (1u << 22); ++it) {
+  const uint32_t limit = reinterpret_cast<const volatile uint32_t *>(abort_flag)[1];
+  for (uint32_t it = 0; it < limit; ++it) {
     if (tc::mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
     if (it > 64) __nanosleep(it > 4096 ? 512 : 32);
@@ -190,6 +197,27 @@ __device__ __forceinline__ bool lag_wait(uint64_t *bar, uint32_t parity, volatil
   *abort_flag = 1;
   atomicExch(err, 1);
   return false;
+}
+
+// The same wait, answered alike on all 32 lanes of the calling warp (every
+// lane must call it): a warp whose lanes took different exits would leave
+// some lanes at a warp-synchronous instruction (tcgen05.ld, elect.sync,
+// __syncwarp) that the others never reach.
+__device__ __forceinline__ bool lag_wait_warp(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err) {
+  const bool ok = lag_wait(bar, parity, abort_flag, err);
+  return __all_sync(0xffffffffu, ok);
+}
+
+// AND of `ok` over the 128 strip-builder threads; also their barrier 1.
+__device__ __forceinline__ bool builders_all(bool ok) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.and.pred po, 1, 128, pi;\n"
+      " selp.u32 %0, 1, 0, po;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)ok)
+      : "memory");
+  return r != 0;
 }
 
 __device__ __forceinline__ int hist_bin_lag(float v, float delta, int n_hist) {
@@ -289,7 +317,7 @@ __global__ void __launch_bounds__(kLagThreads, 1)
   uint64_t *hank_full = bars + 2 * a.stages, *hank_empty = hank_full + 2, *tmem_full = hank_full + 4,
            *tmem_empty = hank_full + 6, *mma_drain = hank_full + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(base + L.misc);
-  volatile int *abort_flag = reinterpret_cast<volatile int *>(base + L.misc + 4);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(base + L.misc + 4);  // + the wait limit at misc + 8
   int *hist = reinterpret_cast<int *>(base + L.hist);
   const bool smem_hist = a.n_hist > 0 && a.n_hist <= kLagHistMax;
 
@@ -308,6 +336,7 @@ __global__ void __launch_bounds__(kLagThreads, 1)
     }
     tc::mbar_init(mma_drain, 1);
     *abort_flag = 0;
+    reinterpret_cast<volatile uint32_t *>(abort_flag)[1] = a.wait_limit ? a.wait_limit : kLagWaitPolls;
     tc::fence_mbarrier_init();
   }
   if (smem_hist)
@@ -346,13 +375,17 @@ __global__ void __launch_bounds__(kLagThreads, 1)
       uint32_t phase = 0;
       long long it = 0;
       uint32_t issued_mask = 0, last_parity = 0;  // per stage: any load issued / parity of the latest
-      for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
+      bool stop = false;  // uniform over the warp
+      for (long long bb = b, qq = q; bb < nblk && !stop; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
         const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
         const long long j_end = min(j_begin + a.jc, n_j);
-        for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp) {
-          for (int c = 0; c < C && !*abort_flag; ++c) {
+        for (long long j0 = j_begin; j0 < j_end && !stop; j0 += a.jp) {
+          for (int c = 0; c < C && !stop; ++c) {
             for (int kc = 0; kc < kchunks; ++kc, ++it) {
-              if (it >= a.stages && !lag_wait(&a_empty[stage], phase ^ 1, abort_flag, a.error_flag)) break;
+              if (it >= a.stages && !lag_wait_warp(&a_empty[stage], phase ^ 1, abort_flag, a.error_flag)) {
+                stop = true;
+                break;
+              }
               if (lane == 0) {
                 unsigned char *dst = base + L.a + stage * nhl * tile_bytes;
                 tc::mbar_arrive_expect_tx(&a_full[stage], nhl * tile_bytes);
@@ -393,14 +426,18 @@ __global__ void __launch_bounds__(kLagThreads, 1)
       const uint32_t strip_u = (uint32_t)a.strip_bytes >> 4;
       const int nnt = a.nt;
       constexpr int kFastGroup = NHL == 1 ? 4 : 2;  // K-chunks of the unrolled group
-      for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
+      bool stop = false;  // uniform over the warp
+      for (long long bb = b, qq = q; bb < nblk && !stop; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
         const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
         const long long j_end = min(j_begin + a.jc, n_j);
-        for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp, ++pass) {
+        for (long long j0 = j_begin; j0 < j_end && !stop; j0 += a.jp, ++pass) {
           const int njp = (int)min((long long)a.jp, j_end - j0);
           const int tb = (int)(pass % a.nbuf);
           const long long tuse = pass / a.nbuf;
-          if (tuse > 0 && !lag_wait(&tmem_empty[tb], (uint32_t)((tuse - 1) & 1), abort_flag, a.error_flag)) break;
+          if (tuse > 0 && !lag_wait_warp(&tmem_empty[tb], (uint32_t)((tuse - 1) & 1), abort_flag, a.error_flag)) {
+            stop = true;
+            break;
+          }
           tc::fence_after_sync();
           const uint32_t tbase = tmem + (uint32_t)tb * buf_cols;
           // (j p, N-tile nt) pairs: TMEM column of the accumulator and the
@@ -413,23 +450,26 @@ __global__ void __launch_bounds__(kLagThreads, 1)
             dcol[cb] = tbase + (uint32_t)(p * a.wpad + nt * a.wt);
             boff[cb] = (uint32_t)(p * nhl) * strip_u + (uint32_t)(nt * (a.wt / 8) * 8);
           }
-          for (int c = 0; c < C && !*abort_flag; ++c, ++unit) {
+          for (int c = 0; c < C && !stop; ++c, ++unit) {
             const int hb = (int)(unit & 1);
-            if (!lag_wait(&hank_full[hb], (uint32_t)((unit >> 1) & 1), abort_flag, a.error_flag)) break;
+            if (!lag_wait_warp(&hank_full[hb], (uint32_t)((unit >> 1) & 1), abort_flag, a.error_flag)) {
+              stop = true;
+              break;
+            }
             tc::fence_after_sync();
             const uint64_t dbu = db0 + (uint64_t)((uint32_t)(hb * a.jp * nhl) * strip_u);
             // K-chunks in groups of `kgroup` ring stages; within a group the
             // MMAs of one K-step offset are issued back to back for every
             // chunk (same accumulator, different operands), which keeps the
             // tensor pipe busier than one chunk's K-steps in a row
-            for (int kc0 = 0; kc0 < kchunks && !*abort_flag; kc0 += a.kgroup) {
+            for (int kc0 = 0; kc0 < kchunks && !stop; kc0 += a.kgroup) {
               const int g = min(a.kgroup, kchunks - kc0);
               bool ok = true;
               {
                 int st = stage;
                 uint32_t ph = phase;
                 for (int t = 0; t < g; ++t) {
-                  if (!lag_wait(&a_full[st], ph, abort_flag, a.error_flag)) {
+                  if (!lag_wait_warp(&a_full[st], ph, abort_flag, a.error_flag)) {
                     ok = false;
                     break;
                   }
@@ -439,7 +479,10 @@ __global__ void __launch_bounds__(kLagThreads, 1)
                   }
                 }
               }
-              if (!ok) break;
+              if (!ok) {
+                stop = true;
+                break;
+              }
               tc::fence_after_sync();
               if (g == kFastGroup && ncombo <= 2) {
                 // the common cases, fully unrolled: a few adds per MMA
@@ -511,16 +554,19 @@ __global__ void __launch_bounds__(kLagThreads, 1)
     asm volatile("bar.sync 1, 128;" ::: "memory");
     const int n8 = a.lp / 8;  // 16-byte chunks per row
     long long unit = 0;
-    for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
+    bool stop = false;  // uniform over the 128 builders
+    for (long long bb = b, qq = q; bb < nblk && !stop; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
       const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
       const long long j_end = min(j_begin + a.jc, n_j);
-      for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp) {
+      for (long long j0 = j_begin; j0 < j_end && !stop; j0 += a.jp) {
         const int njp = (int)min((long long)a.jp, j_end - j0);
-        for (int c = 0; c < C && !*abort_flag; ++c, ++unit) {
+        for (int c = 0; c < C && !stop; ++c, ++unit) {
           const int hb = (int)(unit & 1);
-          // wait until the MMAs of the unit two back (same buffer) no longer read it
-          if (unit >= 2 && !lag_wait(&hank_empty[hb], (uint32_t)(((unit >> 1) - 1) & 1), abort_flag, a.error_flag))
-            break;
+          // wait until the MMAs of the unit two back (same buffer) no longer
+          // read it; its outcome is shared by all builders at the barrier
+          // below (xs, written before it, is the builders' own)
+          const bool ready =
+              unit < 2 || lag_wait(&hank_empty[hb], (uint32_t)(((unit >> 1) - 1) & 1), abort_flag, a.error_flag);
           // rows of the j side (triangle events, or the rectangle's queries):
           // chunks f = ((p * nhl + hl) * n8 + ch), four per thread in flight
           const long long row0 = (long long)c * n_j + j0;
@@ -562,7 +608,10 @@ __global__ void __launch_bounds__(kLagThreads, 1)
               }
             }
           }
-          asm volatile("bar.sync 1, 128;" ::: "memory");
+          if (!builders_all(ready)) {  // also the barrier before the strips are built
+            stop = true;
+            break;
+          }
           for (int p = 0; p < njp; ++p) {
 #pragma unroll
             for (int hl = 0; hl < nhl; ++hl) {
@@ -596,13 +645,17 @@ __global__ void __launch_bounds__(kLagThreads, 1)
     const int e_lane = 32 * quarter + lane;       // event within the block
     const uint32_t lane_addr = (uint32_t)(32 * quarter) << 16;
     long long pass = 0;
-    for (long long bb = b, qq = q; bb < nblk && !*abort_flag; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
+    bool stop = false;  // uniform over the warp
+    for (long long bb = b, qq = q; bb < nblk && !stop; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
       const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
       const long long j_end = min(j_begin + a.jc, n_j);
-      for (long long j0 = j_begin; j0 < j_end && !*abort_flag; j0 += a.jp, ++pass) {
+      for (long long j0 = j_begin; j0 < j_end && !stop; j0 += a.jp, ++pass) {
         const int njp = (int)min((long long)a.jp, j_end - j0);
         const int tb = (int)(pass % a.nbuf);
-        if (!lag_wait(&tmem_full[tb], (uint32_t)((pass / a.nbuf) & 1), abort_flag, a.error_flag)) break;
+        if (!lag_wait_warp(&tmem_full[tb], (uint32_t)((pass / a.nbuf) & 1), abort_flag, a.error_flag)) {
+          stop = true;
+          break;
+        }
         tc::fence_after_sync();
         const long long i = a_row0 + bb * kLagM + e_lane;  // A-side event
         // extrema of the (up to two) j's of the pass, then the TMEM buffer
@@ -660,18 +713,18 @@ __global__ void __launch_bounds__(kLagThreads, 1)
           if (p < njp && (RECT ? (i < a.col_begin + a.n_cols && i < N) : (i < N && j >= i))) {
             const float best = bestp[p], worst = worstp[p];
             const int bn = bnp[p], wn = wnp[p];
-            // final normalisation in FP64: per-event FP64 1/norm (prep kernel)
-            const double *inv = inverse_norms_of(a.norms, N * C);  // A side
-            const double *inv_j = RECT ? inverse_norms_of(a.q_norms, a.n_query * C) : inv;
+            // final normalisation in FP64: per-event 1/norm (FP64, kept as hi + lo)
+            const float2 *inv = inverse_norms_of(a.norms, N * C);  // A side
+            const float2 *inv_j = RECT ? inverse_norms_of(a.q_norms, a.n_query * C) : inv;
             double scale;
             bool live = false;
             if (a.prescaled) {
-              for (int cc = 0; cc < C; ++cc) live |= (inv[i * C + cc] > 0.0) && (inv_j[j * C + cc] > 0.0);
+              for (int cc = 0; cc < C; ++cc) live |= (inv[i * C + cc].x > 0.f) && (inv_j[j * C + cc].x > 0.f);
               scale = 1.0 / (double)C;
             } else {
-              const double ni = inv[i * C], nj = inv_j[j * C];
-              live = ni > 0.0 && nj > 0.0;
-              scale = ni * nj;
+              const float2 ni = inv[i * C], nj = inv_j[j * C];
+              live = ni.x > 0.f && nj.x > 0.f;
+              scale = ((double)ni.x + (double)ni.y) * ((double)nj.x + (double)nj.y);
             }
             float vp = 0.f, vn = 0.f;
             int lp = 0, ln = 0;
@@ -911,6 +964,7 @@ cudaError_t launch_lag_blocks(const void *ws, long long n, int C, int length, in
   a.max_hist = hmax;
   a.min_hist = hmin;
   a.error_flag = error_flag;
+  a.wait_limit = device_wait_polls();
   a.blk_begin = blk_begin;
   a.blk_end = blk_end;
   long long items = 0;
@@ -969,6 +1023,7 @@ cudaError_t launch_lag_rect(const void *cat_ws, long long n_cat, const void *q_w
   a.vals_neg = vn;
   a.lags_neg = ln;
   a.error_flag = error_flag;
+  a.wait_limit = device_wait_polls();
   const long long nblk = (n_cols + kLagM - 1) / kLagM;
   const long long items = nblk * ((n_query + pl.jc - 1) / pl.jc);
   return launch_lag_kernel(a, pl, a.xhi, a.xlo, n_cat * C, items, sm_count, s);

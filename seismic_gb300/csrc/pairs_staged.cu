@@ -28,9 +28,17 @@
 // the critical path.  Row i is staged once per unit for all NG groups:
 // 1 + T rows per T pairs instead of 3 rows per 2.
 //
-// Every mbarrier wait is bounded; one that runs out sets the device error
-// flag and the CTA finishes its items without waiting further (results are
-// then invalid, and the host reports SEISMIC_ERR_DEVICE_TIMEOUT).
+// Bounded waits and the abort path.  The producer's waits (for a slot to be
+// released) are bounded by PairArgs::wait_limit polls; one that runs out sets
+// the device error flag (the host reports SEISMIC_ERR_DEVICE_TIMEOUT; the
+// outputs are then incomplete) and the CTA's abort flag, and the producer
+// issues nothing more.  Before it leaves, the producer waits for every copy
+// it issued to land (copies from valid memory always complete; this wait is
+// bounded too), so the CTA never exits with a copy still writing its shared
+// memory.  The FFT threads poll their `full` barrier and give up only when a
+// unit's copies have not landed AND the abort flag is set, i.e. at a unit
+// the producer never issued; a group leaves its item loop only by a vote of
+// all its threads, so no thread is left waiting at a group barrier.
 #include <cstdlib>
 #include <cstring>
 
@@ -86,17 +94,46 @@ __host__ __device__ __forceinline__ void staged_decode(const PairArgs &a, int T,
   j0 = bj * T;
 }
 
-__device__ __forceinline__ void staged_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err) {
-  if (tc::mbar_try_wait(bar, parity)) return;  // the common case: already complete
-  if (*abort_flag) {
-    (void)tc::mbar_try_wait(bar, parity);
-    return;
-  }
-  if (!tc::mbar_wait(bar, parity)) {
-    *abort_flag = 1;
-    if (err) atomicExch(err, 1);
+// Producer side: bounded wait; on running out it raises the abort and error flags.
+__device__ __forceinline__ bool producer_wait(uint64_t *bar, uint32_t parity, uint32_t limit,
+                                              volatile int *abort_flag, int *err) {
+  if (tc::mbar_wait(bar, parity, limit)) return true;
+  *abort_flag = 1;
+  if (err) atomicExch(err, 1);
+  return false;
+}
+
+// FFT-thread side: true once the phase completed; false only when it has not
+// and the producer has aborted (so it never will).  The phase is tested
+// before the flag: a thread never gives up on a unit that has landed.
+__device__ __forceinline__ bool consumer_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
+  for (uint32_t it = 0;; ++it) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return tc::mbar_try_wait(bar, parity);
+    if (it > 64) __nanosleep(it > 4096 ? 256 : 32);
   }
 }
+
+// True on every thread of the group if `v` is true on any of them.  All G
+// threads of the group must call it (a warp vote, or a named-barrier
+// reduction for groups wider than a warp).
+template <int G> __device__ __forceinline__ bool group_any(int group_in_cta, bool v) {
+  if constexpr (G <= 32) {
+    return __any_sync(group_lane_mask<G>(), v);
+  } else {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.or.pred po, %2, %3, pi;\n"
+        " selp.u32 %0, 1, 0, po;\n}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(group_in_cta + 1), "r"(G)
+        : "memory");
+    return r != 0;
+  }
+}
+
+// Default poll limit of the producer's waits (with back-off: seconds).
+constexpr uint32_t kStagedWaitPolls = 1u << 24;
 
 // Cursor of the next unit to stage (shared memory, used by the producer only).
 struct StagedCursor {
@@ -192,13 +229,24 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       items[0] = StagedItem{cur->i, cur->j0};
       int slot = 0;
       uint32_t phase = 0;
+      const uint32_t limit = a.wait_limit ? a.wait_limit : kStagedWaitPolls;
+      long long issued = 0;
       for (long long u = 0; u < units_total; ++u) {
-        if (u >= K) staged_wait(&empty[slot], phase ^ 1u, s_abort, a.error_flag);
-        if (*s_abort) break;
+        if (u >= K && !producer_wait(&empty[slot], phase ^ 1u, limit, s_abort, a.error_flag)) break;
         staged_issue<P, NWARP, RU, ST>(a, &jmap, cur, items, ring + (size_t)slot * UNIT, &full[slot]);
+        ++issued;
         if (++slot == K) {
           slot = 0;
           phase ^= 1u;
+        }
+      }
+      // drain: the last arming of every slot has landed before the CTA may
+      // exit (immediate when the FFT threads consumed everything)
+      for (int k = 0; k < K && k < issued; ++k) {
+        const long long last = k + ((issued - 1 - k) / K) * K;  // last unit issued into slot k
+        if (!tc::mbar_wait(&full[k], (uint32_t)((last / K) & 1), kStagedWaitPolls)) {
+          *s_abort = 1;
+          if (a.error_flag) atomicExch(a.error_flag, 1);
         }
       }
     }
@@ -217,8 +265,10 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
     uint32_t phase = 0;
     unsigned seq = 0;
     for (long long w = a.couple_begin + blockIdx.x; w < a.couple_end; w += gridDim.x, ++seq) {
-      // the item's first unit being full also publishes its (i, j0)
-      staged_wait(&full[slot], phase, s_abort, a.error_flag);
+      // the item's first unit being full also publishes its (i, j0); if it
+      // never landed, the entry read below is stale, and nothing indexes
+      // memory with it before the group's vote after the unit loop
+      bool stop = !consumer_wait(&full[slot], phase, s_abort);
       const StagedItem it = items[seq % kItemRing];
       const long long i = it.i, j0 = it.j0;
       long long ja = j0 + 2 * g, jb = ja + 1;
@@ -238,10 +288,13 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       const int ra = (1 + (int)(ja - j0)) * S, rb = (1 + (int)(jb - j0)) * S;  // rows of ja, jb in a unit
       CoupleAcc y;
       y.zero();
-      for (int c = 0; c < C; ++c) {
+      for (int c = 0; c < C && !stop; ++c) {
 #pragma unroll
         for (int rp = 0; rp < 8; rp += RU) {
-          staged_wait(&full[slot], phase, s_abort, a.error_flag);
+          if (!consumer_wait(&full[slot], phase, s_abort)) {
+            stop = true;
+            break;
+          }
           const ST_T *u = reinterpret_cast<const ST_T *>(ring + (size_t)slot * UNIT);
 #pragma unroll
           for (int h = 0; h < RU; ++h) {
@@ -255,6 +308,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
           }
         }
       }
+      if (group_any<G>(g, stop)) break;  // aborted inside the item: leave together
       if (live) {  // uniform over the group
         float2 v[32];
         assemble_couple(y, t, v);
@@ -344,6 +398,7 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
     if (e != cudaSuccess) return e;
   }
   a.band_tiles = l2_band_tiles(a.n_channels, P, (int)sizeof(ST_T), SH::T);
+  a.wait_limit = device_wait_polls();
 
   // Tensor map of the j spectra: dims {P/2 bins, C channels, N events},
   // box {S bins, 1 channel, T events}.

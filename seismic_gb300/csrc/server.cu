@@ -14,6 +14,17 @@
 //      kernel (queries x catalog subset) -> top-K kernel -> D2H outputs ->
 //      host callback (completion time, frees slot + memory).
 //    Requests in different slots run concurrently on the device.
+//  * The rectangular pair kernel is persistent (one CTA per SM, nearly all
+//    of an SM's shared memory), so two of them interleave only at CTA
+//    boundaries, and a kernel launched behind one would take every SM the
+//    first one frees -- including the SMs the first request's own top-K
+//    kernel needs, which would then wait for the whole second kernel.  So
+//    the pair kernels of admitted requests run in admission order (each
+//    waits on the previous one's completion event), on all but `spare_sms`
+//    SMs; the other stages of every request in flight (H2D, query
+//    transform, top-K, D2H) run beside them on the spare SMs and the copy
+//    engines.  A request finishes one pair-kernel time after the one ahead
+//    of it, and the device never idles between requests.
 //  * seismic_server_wait blocks until a ticket completes and returns its
 //    latency (submit -> results in host memory).
 // Results do not depend on what else is in flight: every request has its own
@@ -153,11 +164,18 @@ struct seismic_server {
   int *error_flag = nullptr;  // device flag set by a bounded wait that ran out
   int max_query = 64;
   // A request joins others already on the device only when at least this
-  // many requests wait (counting it): at light load each request runs alone
-  // (lowest latency), under backlog they overlap (highest throughput).
-  // SEISMIC_SERVER_OVERLAP_BACKLOG, default 2; 1 overlaps whenever a slot
-  // is free.
-  int overlap_backlog = 2;
+  // many requests wait (counting it).  Default 1: admitted whenever a slot
+  // and pool memory are free (continuous batching);
+  // SEISMIC_SERVER_OVERLAP_BACKLOG=2 holds a lone arrival until the device
+  // is idle.
+  int overlap_backlog = 1;
+  // SMs the pair kernels leave to the other stages of requests in flight
+  // (SEISMIC_SERVER_SPARE_SMS, default 2).
+  int spare_sms = 2;
+  // completion of each slot's pair kernel, and the most recent one enqueued
+  // (the next pair kernel waits on it); dispatcher thread only
+  std::vector<cudaEvent_t> pair_done;
+  cudaEvent_t last_pair = nullptr;
   // pool
   char *pool = nullptr;
   size_t pool_bytes = 0;
@@ -243,6 +261,12 @@ void CUDART_CB on_complete(void *p) {
   s->cv_dispatch.notify_one();
 }
 
+// SMs the pair kernels of requests run on.
+int pair_sms(const seismic_server *s) {
+  const int n = s->sm_count - s->spare_sms;
+  return n > 0 ? n : 1;
+}
+
 // Enqueue the whole pipeline of `r` on its slot's stream (dispatcher thread).
 int launch_request(seismic_server *s, Request *r) {
   cudaStream_t st = s->streams[r->slot];
@@ -277,9 +301,10 @@ int launch_request(seismic_server *s, Request *r) {
   if (s->lag_form) {  // time-domain lag sums on the tensor cores
     if (e == cudaSuccess)
       e = lag_prepare(q_ev, nq, s->C, s->L, (long long)s->C * s->L, s->L, s->lag_form, q_spec, st);
+    if (e == cudaSuccess && s->last_pair) e = cudaStreamWaitEvent(st, s->last_pair, 0);
     if (e == cudaSuccess)
       e = launch_lag_rect(s->cat_lag, s->n_cat, q_spec, nq, s->C, s->L, s->shift, r->col_begin, r->n_cols,
-                          s->threshold, s->lag_form, d_vp, d_lp, d_vn, d_ln, s->error_flag, s->sm_count, st);
+                          s->threshold, s->lag_form, d_vp, d_lp, d_vn, d_ln, s->error_flag, pair_sms(s), st);
     note_launches(2);
   } else {
   SpectraArgs sa{};
@@ -322,8 +347,11 @@ int launch_request(seismic_server *s, Request *r) {
   pa.error_flag = s->error_flag;
   pa.couple_begin = 0;
   pa.couple_end = pair_work_total(s->P, pa);
-  if (e == cudaSuccess) e = launch_pair_work(s->P, pa, s->sm_count, 0, st);
+  if (e == cudaSuccess && s->last_pair) e = cudaStreamWaitEvent(st, s->last_pair, 0);
+  if (e == cudaSuccess) e = launch_pair_work(s->P, pa, pair_sms(s), 0, st);
   }
+  if (e == cudaSuccess) e = cudaEventRecord(s->pair_done[r->slot], st);
+  if (e == cudaSuccess) s->last_pair = s->pair_done[r->slot];
   if (e == cudaSuccess && s->topk > 0) {
     topk_kernel<<<nq, kTopKThreads, 0, st>>>(d_vp, r->n_cols, s->topk, r->col_begin, d_tv, d_ti);
     e = cudaGetLastError();
@@ -434,6 +462,10 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
     const int v = atoi(env);
     if (v >= 1) s->overlap_backlog = v;
   }
+  if (const char *env = getenv("SEISMIC_SERVER_SPARE_SMS")) {
+    const int v = atoi(env);
+    if (v >= 0 && v < sm) s->spare_sms = v;
+  }
   const long long rows = n_catalog * n_channels;
   float *d_cat = nullptr;
   cudaError_t e = cudaSuccess;
@@ -486,8 +518,10 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   }
   s->free_list[0] = s->pool_bytes;
   s->streams.resize(n_slots);
+  s->pair_done.resize(n_slots);
   s->slot_busy.assign(n_slots, false);
   for (auto &st : s->streams) cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+  for (auto &ev : s->pair_done) cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   // make sure the pair kernel's attributes are set before concurrent use
   pair_ctas_per_sm(P);
   int dev = 0;
@@ -592,6 +626,7 @@ extern "C" int seismic_server_destroy(seismic_server *s) {
   s->cv_dispatch.notify_all();
   if (s->dispatcher.joinable()) s->dispatcher.join();
   for (auto &st : s->streams) cudaStreamDestroy(st);
+  for (auto &ev : s->pair_done) cudaEventDestroy(ev);
   for (auto &kv : s->by_ticket) delete kv.second;
   cudaFree(s->cat_spectra);
   cudaFree(s->cat_norms);

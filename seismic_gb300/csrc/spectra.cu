@@ -178,10 +178,10 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
     const double ia = na > 0.0 ? 1.0 / na : 0.0;
     const double ib = nb > 0.0 ? 1.0 / nb : 0.0;
     a.norms[row_a] = na;
-    a.inv_norms[row_a] = ia;
+    a.inv_norms[row_a] = split_double(ia);
     if (has_b) {
       a.norms[row_b] = nb;
-      a.inv_norms[row_b] = ib;
+      a.inv_norms[row_b] = split_double(ib);
     }
     float *scale = reinterpret_cast<float *>(red);
     scale[0] = a.prescale ? (float)ia : 1.f;

@@ -67,7 +67,7 @@ def test_cuda_dropin_module_as_the_reference_driver_imports_it(cuda_ok, tmp_path
     np.save(tmp_path / "events.npy", g["events"])
     script = (
         "import sys, numpy as np\n"
-        f"sys.path.insert(0, {os.path.join(O.ROOT, 'seismic_gb300', 'cuda')!r})\n"
+        f"sys.path.insert(0, {os.path.join(root, 'seismic_gb300', 'cuda')!r})\n"
         "from correlation_lib import compute_correlation, initialiseRunTime\n"
         "initialiseRunTime()\n"
         f"ev = np.load({str(tmp_path / 'events.npy')!r})\n"
