@@ -84,6 +84,25 @@ def fft_flops_per_pair(p: int, c: int) -> float:
     return 2.5 * p * np.log2(p) + 6.0 * c * (p // 2 + 1)
 
 
+def fft_plan(lib, length: int, shift: int, p: int, c: int, form_code: int) -> dict:
+    """The transform the library runs for these sizes (seismic_fft_plan):
+    the plain size-P form (blocks 0) or the overlap-save frames."""
+    q, b, bl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    from seismic_gb300 import _lib
+    _lib.check(lib.seismic_fft_plan(length, shift, p, c, form_code, ctypes.byref(q), ctypes.byref(b),
+                                    ctypes.byref(bl)))
+    return {"transform_size": q.value, "blocks": b.value, "block_length": bl.value}
+
+
+def executed_flops_per_pair(plan: dict, p: int, c: int) -> float:
+    """FLOPs per pair of the transform the kernel runs: the plain count, or
+    one size-Q inverse FFT plus C x blocks conj-products of Q/2+1 bins."""
+    if not plan or plan["blocks"] == 0:
+        return fft_flops_per_pair(p, c)
+    q = plan["transform_size"]
+    return 2.5 * q * np.log2(q) + 6.0 * c * plan["blocks"] * (q // 2 + 1)
+
+
 # arithmetic type of each form's products (accumulation is FP32 in all of them)
 FORM_DTYPE = {"fp32": "f32", "fp16": "f16", "bf16": "bf16", "laggemm": "bf16x3 (hi+lo)", "laggemm16": "f16"}
 
@@ -332,27 +351,32 @@ def measure_lag_form(lib, form, d_ev, ev, shift, outs, hist, flush, stream, args
     lag_ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
     vp, lp, vn, ln = outs
 
-    def call():
-        _lib.check(lib.seismic_xcorr_device(d_ev.data_ptr(), n, c, length, c * length, length, 0, shift, 0.0, 20,
-                                            code, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(), ln.data_ptr(),
-                                            hist[0].data_ptr(), hist[1].data_ptr(), lag_ws.data_ptr(), wsb,
-                                            ctypes.c_void_p(stream.cuda_stream)))
+    def call(stage):  # 1: prep (16-bit planes + FP64 norms), 2: the lag-GEMM
+        _lib.check(lib.seismic_xcorr_device_stages(d_ev.data_ptr(), n, c, length, c * length, length, 0, shift, 0.0,
+                                                   20, code, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(),
+                                                   ln.data_ptr(), hist[0].data_ptr(), hist[1].data_ptr(),
+                                                   lag_ws.data_ptr(), wsb, ctypes.c_void_p(stream.cuda_stream),
+                                                   stage))
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            call()
+            call(1)
+            call(2)
     torch.cuda.synchronize(dev)
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(3 * args.steps)]
     launches0 = lib.seismic_launch_count()
     with torch.cuda.stream(stream):
         for k in range(args.steps):
             flush.zero_()
             hist.zero_()
-            evs[2 * k].record(stream)
-            call()
-            evs[2 * k + 1].record(stream)
+            evs[3 * k].record(stream)
+            call(1)
+            evs[3 * k + 1].record(stream)
+            call(2)
+            evs[3 * k + 2].record(stream)
     torch.cuda.synchronize(dev)
     launches = lib.seismic_launch_count() - launches0
-    t = np.array([evs[2 * k].elapsed_time(evs[2 * k + 1]) for k in range(args.steps)]) * 1e-3
+    t = np.array([evs[3 * k].elapsed_time(evs[3 * k + 2]) for k in range(args.steps)]) * 1e-3
+    t_gemm = float(np.mean([evs[3 * k + 1].elapsed_time(evs[3 * k + 2]) for k in range(args.steps)])) * 1e-3
     step = float(t.mean())
     if ws > 1:
         import torch.distributed as dist
@@ -364,7 +388,7 @@ def measure_lag_form(lib, form, d_ev, ev, shift, outs, hist, flush, stream, args
     fp64 = fp64_sample_error(ev, shift, p_lin, vp.cpu().numpy(), lp.cpu().numpy(), vn.cpu().numpy(),
                              ln.cpu().numpy(), n_sample=4000)
     flops = npairs * c * 2.0 * length * (2 * shift)
-    achieved = flops / step / 1e12
+    achieved = flops / t_gemm / 1e12
     peak = peaks.get("bf16_tflops_sustained", 1700.0)
     products = 3 if form == "laggemm" else 1
     out = {"form": FORM_TEXT[form], "dtype": FORM_DTYPE[form], "value": value, "unit": "pairs/s",
@@ -376,7 +400,8 @@ def measure_lag_form(lib, form, d_ev, ev, shift, outs, hist, flush, stream, args
                         "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured): a kernel timed "
                                        "inside a step of tens of ms" if "bf16_tflops_sustained" in peaks
                         else "fallback 1.7 PFLOP/s sustained",
-                        "kernel": "lag_gemm_kernel (+ lag_prep_kernel, < 1 % of the step)",
+                        "kernel": "lag_gemm_kernel, timed alone", "kernel_ms": t_gemm * 1e3,
+                        "kernel_share_of_step": t_gemm / step,
                         "work": f"{npairs} pairs x {c} ch x 2 L (2 shift) flop, L={length}, shift={shift}"},
            "gpu_launches": int(launches), "e2e": None}
     if host is not None:
@@ -401,11 +426,8 @@ def run_ours(args):
     p = 1 << int(length).bit_length()
     npairs = n * (n + 1) // 2
     rows = n * c
-    prescale = 1 if c > 1 else 0
 
     d_ev = torch.from_numpy(ev).to(dev)
-    spectra = torch.empty(rows * (p // 2) * 2, dtype=torch.float32, device=dev)
-    norms = torch.empty(2 * rows, dtype=torch.float64, device=dev)  # FP64 norms + FP64 inverse norms
     vp = torch.empty(npairs, dtype=torch.float32, device=dev)
     lp = torch.empty(npairs, dtype=torch.int32, device=dev)
     vn = torch.empty(npairs, dtype=torch.float32, device=dev)
@@ -416,30 +438,27 @@ def run_ours(args):
     sh = ctypes.c_void_p(stream.cuda_stream)
 
     form_code = _lib.FORMS[args.form]
-    if args.form == "fp32":
-        def spectra_call():
-            _lib.check(lib.seismic_spectra_device(d_ev.data_ptr(), n, c, length, c * length, length, p, prescale,
-                                                  spectra.data_ptr(), norms.data_ptr(), sh))
+    lag = args.form.startswith("laggemm")
+    p_arg = 0 if lag else p
+    wsb = lib.seismic_xcorr_workspace_bytes(n, c, length, shift, p_arg, form_code)
+    if wsb == 0:
+        raise SystemExit(f"form {args.form} does not support this workload")
+    ws_t = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    plan = None if lag else fft_plan(lib, length, shift, p, c, form_code)
 
-        def pairs_call():
-            _lib.check(lib.seismic_pairs_device(spectra.data_ptr(), norms.data_ptr(), n, c, p, prescale, shift, 0.0,
-                                                20, 0, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(), ln.data_ptr(),
-                                                hist[0].data_ptr(), hist[1].data_ptr(), sh))
-    else:  # forms run as one call: spectra + pairs (fp16/bf16) or prep + lag-GEMM
-        wsb = lib.seismic_xcorr_workspace_bytes(n, c, length, shift, p if not args.form.startswith("laggemm") else 0, form_code)
-        if wsb == 0:
-            raise SystemExit(f"form {args.form} does not support this workload")
-        lag_ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    # the two halves of seismic_xcorr_device, timed apart: kernel (a) (spectra
+    # + FP64 norms, or the lag form's planes) and kernel (b) (all pairs)
+    def stage_call(stage):
+        _lib.check(lib.seismic_xcorr_device_stages(d_ev.data_ptr(), n, c, length, c * length, length, p_arg, shift,
+                                                   0.0, 20, form_code, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(),
+                                                   ln.data_ptr(), hist[0].data_ptr(), hist[1].data_ptr(),
+                                                   ws_t.data_ptr(), wsb, sh, stage))
 
-        def spectra_call():  # the lag-GEMM form has no separate spectra step
-            return None
+    def spectra_call():
+        stage_call(1)
 
-        def pairs_call():
-            _lib.check(lib.seismic_xcorr_device(d_ev.data_ptr(), n, c, length, c * length, length,
-                                                p if not args.form.startswith("laggemm") else 0, shift, 0.0, 20,
-                                                form_code, vp.data_ptr(), lp.data_ptr(), vn.data_ptr(),
-                                                ln.data_ptr(), hist[0].data_ptr(), hist[1].data_ptr(),
-                                                lag_ws.data_ptr(), wsb, sh))
+    def pairs_call():
+        stage_call(2)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -508,13 +527,20 @@ def run_ours(args):
         sm_count = torch.cuda.get_device_properties(dev).multi_processor_count
         sm_mhz = clk.get("sm_mhz") or 2070.0
         peak_tf = sm_count * 128 * 2 * sm_mhz * 1e6 / 1e12
+        executed_tf = npairs * executed_flops_per_pair(plan, p, c) / t_pair_mean / 1e12
         roofline = {"bound": "fp32", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
                     "frac": achieved_tf / peak_tf,
                     "traffic": (traffic_pp * npairs) if traffic_pp is not None else None,
                     "kernel": pair_kernel_name(p, c),
                     "peak_source": f"nominal FP32 FMA rate: {sm_count} SMs x 128 lanes x 2 flop x median SM clock "
                                    f"{sm_mhz:.0f} MHz under load (MEASURED_PEAKS.json has no FP32 figure)",
-                    "work": f"{npairs} pairs x (2.5 P log2 P + 6 C (P/2+1)) flop, P={p}, C={c}",
+                    "work": f"{npairs} pairs x (2.5 P log2 P + 6 C (P/2+1)) flop, P={p}, C={c} (the reference's "
+                            "size-P transform per pair, counted whatever transform runs)",
+                    "transform": plan,
+                    "executed_work": "as work" if not plan["blocks"] else
+                    f"{npairs} pairs x (2.5 Q log2 Q + 6 C nb (Q/2+1)) flop, Q={plan['transform_size']}, "
+                    f"nb={plan['blocks']} overlap-save frames of {plan['block_length']} samples",
+                    "executed_achieved": executed_tf, "executed_frac": executed_tf / peak_tf,
                     "pair_kernel_ms": t_pair_mean * 1e3, "pair_kernel_share_of_step": t_pair_mean / step_mean}
     else:  # lag-GEMM: tensor pipe; algorithmic work 2 L (2 shift) per channel-pair, hi/lo extras not counted
         flops = npairs * c * 2.0 * length * (2 * shift)
@@ -523,14 +549,16 @@ def run_ours(args):
         roofline = {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
                     "frac": achieved_tf / peak_tf,
                     "traffic": (traffic_pp * npairs) if traffic_pp is not None else None,
-                    "kernel": "lag_gemm_kernel (+ lag_prep_kernel, < 1 % of the step)",
+                    "kernel": "lag_gemm_kernel (timed alone; lag_prep_kernel is the step's other launch)",
                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst) of measured" if "bf16_tflops" in peaks
                     else "fallback 1.9 PFLOP/s",
                     "work": f"{npairs} pairs x {c} ch x 2 L (2 shift) flop, L={length}, shift={shift}; "
                             + ("the three BF16 hi/lo products issue 3x this on the tensor pipe"
                                if args.form == "laggemm" else "one FP16 product per lag sum"),
                     "pair_kernel_ms": t_pair_mean * 1e3, "pair_kernel_share_of_step": t_pair_mean / step_mean}
-    spec_bytes = rows * (length * 4 + (p // 2) * 8 + 8)
+    # kernel (a): samples in, spectra (plain, or A + W frames) and 16 B of norms out
+    spec_out = (p // 2) * 8 if not plan or not plan["blocks"] else 2 * plan["blocks"] * (plan["transform_size"] // 2) * 8
+    spec_bytes = rows * (length * 4 + spec_out + 16)
     spectra_roof = None
     if args.form == "fp32":
         spectra_roof = {"bound": "hbm", "achieved": spec_bytes / float(t_spec.mean()) / 1e9, "unit": "GB/s",
@@ -546,7 +574,7 @@ def run_ours(args):
            "data": "synthetic: seeded family-based waveforms (no public dataset; the reference's is not distributed)",
            "config": {"workload": args.workload + ": " + workload_text(args.workload, args.form), "n_events": n,
                       "n_channels": c, "event_length": length, "shift": shift, "padded_size": p,
-                      "pairs_per_step": npairs, "form": args.form,
+                      "pairs_per_step": npairs, "form": args.form, "transform": plan,
                       "l2": "L2 flushed (256 MB write) between timed steps; spectra > L2 for this workload"
                       if rows * p * 4 > 129e6 else "L2 flushed (256 MB write) between timed steps"},
            "fp64_error": fp64, "roofline": roofline, "spectra_kernel": spectra_roof, "e2e": e2e,
@@ -581,29 +609,9 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def _catalog_job(job):
-    n, c, length, s = job
-    return synth.family_catalog(n, c, length, n_families=max(1, n // 32), seed=s)
-
-
 def batched_catalogs(n_catalogs: int = 256, seed: int = 4000):
-    """Seeded catalogs of the batched workload: (events (N, C, L), shift).
-    Generated in a spawn-context process pool (each catalog has its own seed,
-    so the result does not depend on the pool)."""
-    import concurrent.futures as cf
-    import multiprocessing as mp
-    rng = np.random.default_rng(seed)
-    lengths = [256, 512, 1000, 2048, 3000, 4096]
-    jobs = []
-    for k in range(n_catalogs):
-        n = int(round(np.exp(rng.uniform(np.log(16), np.log(2048)))))
-        length = int(rng.choice(lengths))
-        c = int(rng.choice([1, 3]))
-        jobs.append((n, c, length, seed + 1 + k))
-    workers = max(1, min(16, len(os.sched_getaffinity(0))))
-    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
-        evs = list(ex.map(_catalog_job, jobs, chunksize=4))
-    return [(ev, job[2]) for ev, job in zip(evs, jobs)]
+    """Seeded catalogs of the batched workload: [(events (N, C, L), shift)]."""
+    return synth.batched_catalogs(n_catalogs, seed)
 
 
 def run_batched(args):
@@ -740,27 +748,16 @@ def run_batched(args):
         dist.destroy_process_group()
 
 
-def _serving_chunk(job):
-    n, s = job
-    return synth.family_catalog(n, 3, 1024, n_families=max(1, n // 32), seed=s)
-
-
 def run_serving(args):
     """Serving form: 50,000 x 3 x 1024 resident catalog, lags -255..256,
     Poisson query stream; reports latency percentiles and pairs/s."""
-    import concurrent.futures as cf
-    import multiprocessing as mp
-    import threading
     import torch
     from seismic_gb300 import _lib
     from seismic_gb300.serving import Server
 
-    torch.cuda.set_device(0)
     n_cat = args.n_events or 50000
-    jobs = [(min(2500, n_cat - b), 9000 + b) for b in range(0, n_cat, 2500)]
-    with cf.ProcessPoolExecutor(max_workers=max(1, min(16, len(os.sched_getaffinity(0)))),
-                                mp_context=mp.get_context("spawn")) as ex:
-        cat = np.concatenate(list(ex.map(_serving_chunk, jobs)))
+    cat = synth.serving_catalog(n_cat)  # process pool: before the first GPU call
+    torch.cuda.set_device(0)
     shift = 256
     form = args.form if args.form in ("fp32", "fp16", "laggemm", "laggemm16") else "fp16"
     lib = _lib.lib()

@@ -121,6 +121,18 @@ int seismic_resolve_padded_size(int event_length, int shift);
 size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int event_length, int shift,
                                      int padded_size, int form);
 
+/* The transform seismic_xcorr_device / seismic_xcorr_host run for these
+ * sizes in an FFT form: *transform_size = padded_size and *blocks = 0 for
+ * the plain form (one size-P transform per event), or, for a short lag
+ * window, the overlap-save form: *blocks frames of *transform_size points
+ * per event, each covering *block_length samples plus `shift` on either
+ * side, whose correlations sum to the same linear correlation at fewer
+ * FLOPs per pair.  padded_size 0 = seismic_resolve_padded_size.  No
+ * counterpart in the reference (always one size-P transform,
+ * correlation_c.cpp:39-45). */
+int seismic_fft_plan(int event_length, int shift, int padded_size, int n_channels, int form, int *transform_size,
+                     int *blocks, int *block_length);
+
 /* Returns SEISMIC_OK, or SEISMIC_ERR_DEVICE_TIMEOUT if a kernel of this
  * library gave up a bounded wait since the last check (and clears the flag).
  * Synchronises the current device.  Allocates nothing (no stream, no
@@ -143,6 +155,21 @@ int seismic_xcorr_device(const float *d_events, long long n_events, int n_channe
                          float threshold, int n_classes_hist, int form, float *d_vals_pos,
                          int *d_lags_pos, float *d_vals_neg, int *d_lags_neg, int *d_max_hist,
                          int *d_min_hist, void *workspace, size_t workspace_bytes, void *stream);
+
+/* seismic_xcorr_device in two halves over the caller's workspace: stages = 1
+ * runs the per-event transforms into the workspace (kernel (a): spectra and
+ * FP64 norms, or the lag-GEMM form's sample planes), stages = 2 the pairs
+ * from it (kernel (b)), 3 both.  The workspace must stay untouched between
+ * the two calls, which take the same arguments; reusing one stage-1 result
+ * for several stage-2 calls (other thresholds or histogram sizes) is
+ * allowed.  The output pointers are not read by stage 1.  No counterpart in
+ * the reference, whose correlationCPP (correlation_c.cpp:210) runs both in
+ * one call. */
+int seismic_xcorr_device_stages(const float *d_events, long long n_events, int n_channels, int event_length,
+                                long long event_stride, long long channel_stride, int padded_size, int shift,
+                                float threshold, int n_classes_hist, int form, float *d_vals_pos, int *d_lags_pos,
+                                float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist,
+                                void *workspace, size_t workspace_bytes, void *stream, int stages);
 
 /* Same computation from host memory (pinned or pageable) into host memory,
  * synchronous: copies events in, runs, copies the packed outputs back and
@@ -193,7 +220,10 @@ long long seismic_pair_couples(long long n_events, int padded_size, int n_channe
  * the GPU's memory for its own pool, a process under a fixed device-memory
  * quota, or a latency-critical loop that cannot afford an allocation's
  * implicit synchronisation.  Arguments and results are those of
- * seismic_xcorr_device (FP32 form, no workspace argument); the scratch for
+ * seismic_xcorr_device (FP32 form, no workspace argument), always through
+ * the plain size-P transform (where seismic_xcorr_device takes the
+ * overlap-save form of a short lag window, the two agree to the parity
+ * bar: 1e-5 on coefficients, lags up to FP32 ties); the scratch for
  * the spectra and norms is one fixed array of seismic_noalloc_scratch_bytes()
  * (64 MiB) inside this library, reserved on every device that uses it until
  * the process exits.  Catalogs needing more than that

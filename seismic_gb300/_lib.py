@@ -48,10 +48,16 @@ def _declare(lib):
         "seismic_xcorr_workspace_bytes": (ctypes.c_size_t, [c_ll, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                             ctypes.c_int, ctypes.c_int]),
         "seismic_check_device_error": (ctypes.c_int, []),
+        "seismic_fft_plan": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            c_int_p, c_int_p, c_int_p]),
         "seismic_xcorr_device": (ctypes.c_int, [vp, c_ll, ctypes.c_int, ctypes.c_int, c_ll, c_ll,
                                                 ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                 ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp,
                                                 vp, ctypes.c_size_t, vp]),
+        "seismic_xcorr_device_stages": (ctypes.c_int, [vp, c_ll, ctypes.c_int, ctypes.c_int, c_ll, c_ll,
+                                                       ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                       ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp,
+                                                       vp, ctypes.c_size_t, vp, ctypes.c_int]),
         "seismic_xcorr_host": (ctypes.c_int, [vp, c_ll, ctypes.c_int, ctypes.c_int, c_ll, c_ll,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                               ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp, vp]),

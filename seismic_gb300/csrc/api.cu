@@ -129,6 +129,74 @@ static size_t spectra_bytes(long long rows, int P, int stype = 0) {
 }
 static size_t norms_bytes(long long rows) { return norms_buffer_bytes(rows); }
 
+// Overlap-save plan of a short lag window (declared in kernels.cuh).  The
+// pair cost of a transform size is its inverse FFT plus the conj-products
+// of every spectrum row, 2.5 Q log2 Q + 6 C nb (Q/2) flop per pair; a block
+// form is chosen when it costs under 3/4 of the plain size-P form.  Only
+// where the plain form has no circular aliasing (L + shift <= P), so both
+// compute the same linear correlation, and only for the sizes of the staged
+// pair form (it has no direct-load twin).  SEISMIC_BLOCK_FORM=off keeps the
+// plain form.
+BlockPlan block_plan(int length, int shift, int P, int n_channels, int stype) {
+  BlockPlan best;
+  const char *env = getenv("SEISMIC_BLOCK_FORM");
+  if ((env && strcmp(env, "off") == 0) || !staged_enabled()) return best;
+  if (stype < 0 || stype > 2 || shift < 1 || (long long)length + shift > P) return best;
+  auto cost = [&](int q, int nb) {
+    return 2.5 * q * (31 - __builtin_clz((unsigned)q)) + 6.0 * n_channels * nb * (q / 2);
+  };
+  double best_cost = 0.75 * cost(P, 1);
+  for (int q = 512; q <= 4096 && q < P; q <<= 1) {
+    const int b = q - 2 * shift;  // B + 2 shift <= Q
+    if (b < q / 8) continue;      // blocks too short to pay for their frames
+    const int nb = (length + b - 1) / b;
+    const double c = cost(q, nb);
+    if (c < best_cost) {
+      best_cost = c;
+      best.Q = q;
+      best.B = b;
+      best.nb = nb;
+    }
+  }
+  return best;
+}
+
+// Workspace layout of an FFT form on one catalog: plain size-P spectra + norms,
+// or the overlap-save A frames, W frames + norms.
+struct FftJob {
+  int P = 0;          // transform size of the pair kernel (Q in the overlap-save form)
+  int stype = 0;
+  int C = 1;
+  int L = 0;
+  int shift = 0;
+  BlockPlan bp;       // bp.nb == 0: plain
+  long long n = 0;
+  size_t spec_b = 0;  // one spectra array (plain or A), 256-byte aligned
+  int prescale = 0;
+  int spec_rows() const { return bp.nb ? C * bp.nb : C; }
+  size_t total() const { return (bp.nb ? 2 : 1) * spec_b + norms_bytes(n * C); }
+  void *spectra(void *ws) const { return ws; }  // plain, or A frames
+  void *spectra_w(void *ws) const { return bp.nb ? static_cast<char *>(ws) + spec_b : nullptr; }
+  double *norms(void *ws) const {
+    return reinterpret_cast<double *>(static_cast<char *>(ws) + (bp.nb ? 2 : 1) * spec_b);
+  }
+};
+
+static FftJob fft_job(long long n, int C, int L, int shift, int P, int stype) {
+  FftJob j;
+  j.n = n;
+  j.C = C;
+  j.L = L;
+  j.shift = shift;
+  j.stype = stype;
+  j.bp = block_plan(L, shift, P, C, stype);
+  j.P = j.bp.nb ? j.bp.Q : P;
+  j.spec_b = spectra_bytes(n * C * (j.bp.nb ? j.bp.nb : 1), j.P, stype);
+  // half-precision spectra are always scaled by 1/norm (keeps |X| <= sqrt(L))
+  j.prescale = (C > 1 || stype != 0) ? 1 : 0;
+  return j;
+}
+
 static bool is_lag_form(int form) {
   return form == SEISMIC_FORM_LAGGEMM_BF16X3 || form == SEISMIC_FORM_LAGGEMM_FP16;
 }
@@ -184,9 +252,11 @@ static int run_spectra(const DeviceState &st, const float *d_events, long long n
 static int run_pairs(const DeviceState &st, const void *spectra, const double *norms, long long n, int C, int P,
                      int prescaled, int shift, float thr, int n_hist, float *vp, int *lp, float *vn, int *ln,
                      int *hmax, int *hmin, cudaStream_t stream, int stype = 0, long long range_begin = 0,
-                     long long range_end = -1) {
+                     long long range_end = -1, const void *spectra_i = nullptr, int spec_rows = 0) {
   PairArgs pa{};  // zero: triangle mode, no query spectra
   pa.spectra = spectra;
+  pa.spectra_i = spectra_i;
+  pa.spec_channels = spec_rows;
   pa.stype = stype;
   pa.norms = norms;
   pa.inv_norms = inverse_norms_of(norms, n * C);
@@ -224,6 +294,7 @@ long long pair_work_total(int P, const PairArgs &a) {
 cudaError_t launch_pair_work(int P, const PairArgs &a, int sm_count, int ctas_per_sm, cudaStream_t stream) {
   if (a.couple_end <= a.couple_begin) return cudaSuccess;
   if (staged_supported(P, a)) return launch_pairs_staged(P, a, sm_count, stream);
+  if (a.spectra_i) return cudaErrorNotSupported;  // overlap-save frames: staged form only
   PairArgs d = a;  // direct form: L2 row bands of tiles (triangle mode)
   if (!d.rect && d.band_tiles == 0) d.band_tiles = l2_band_tiles(d.n_channels, P, d.stype ? 4 : 8, d.tile);
   const int occ = pair_ctas_per_sm_cached(P);
@@ -272,9 +343,12 @@ int pair_ctas_per_sm_cached(int P) {
 struct PairBandPlan {
   long long tile_side, items_per_tile, nb, band;
 };
-static PairBandPlan pair_band_plan(int P, const void *spectra, int stype, long long n, int C) {
+static PairBandPlan pair_band_plan(int P, const void *spectra, int stype, long long n, int C,
+                                   const void *spectra_i = nullptr, int spec_rows = 0) {
   PairArgs a{};
   a.spectra = spectra;
+  a.spectra_i = spectra_i;
+  a.spec_channels = spec_rows;
   a.stype = stype;
   a.n_events = n;
   a.n_channels = C;
@@ -288,7 +362,7 @@ static PairBandPlan pair_band_plan(int P, const void *spectra, int stype, long l
     b.items_per_tile = (long long)a.tile * a.tile / 2;
   }
   b.nb = (n + b.tile_side - 1) / b.tile_side;
-  b.band = l2_band_tiles(C, P, stype ? 4 : 8, (int)b.tile_side);
+  b.band = l2_band_tiles(spectrum_rows(a), P, stype ? 4 : 8, (int)b.tile_side);
   return b;
 }
 // First event row of band k (n past the last band).
@@ -296,6 +370,53 @@ static long long band_row(const PairBandPlan &b, long long k, long long n) {
   const long long band = (b.band <= 0 || b.band > b.nb) ? b.nb : b.band;
   const long long r = k * band * b.tile_side;
   return r < n ? r : n;
+}
+
+// Kernel (a) of an FFT job: plain spectra, or the overlap-save frames.
+static int run_fft_spectra(const DeviceState &st, const FftJob &job, const float *d_events, long long ev_stride,
+                           long long ch_stride, void *ws, cudaStream_t stream) {
+  if (!job.bp.nb)
+    return run_spectra(st, d_events, job.n, job.C, job.L, ev_stride, ch_stride, job.P, job.prescale,
+                       job.spectra(ws), job.norms(ws), stream, job.stype);
+  SpectraArgs sa{};
+  sa.events = d_events;
+  sa.n_events = job.n;
+  sa.n_channels = job.C;
+  sa.length = job.L;
+  sa.ev_stride = ev_stride;
+  sa.ch_stride = ch_stride;
+  sa.prescale = job.prescale;
+  sa.stype = job.stype;
+  sa.spectra = job.spectra(ws);
+  sa.spectra_w = job.spectra_w(ws);
+  sa.norms = job.norms(ws);
+  sa.inv_norms = inverse_norms_of(sa.norms, job.n * job.C);
+  sa.twiddles = st.twiddles;
+  sa.blocks = job.bp.nb;
+  sa.block_len = job.bp.B;
+  sa.block_shift = job.shift;
+  SEISMIC_TRY(launch_block_spectra(job.P, sa, stream), "overlap-save spectra kernel launch");
+  g_launches.fetch_add(1);
+  return SEISMIC_OK;
+}
+
+// Kernel (b) of an FFT job over work items [range_begin, range_end).
+static int run_fft_pairs(const DeviceState &st, const FftJob &job, void *ws, float thr, int n_hist, float *vp,
+                         int *lp, float *vn, int *ln, int *hmax, int *hmin, cudaStream_t stream,
+                         long long range_begin = 0, long long range_end = -1) {
+  if (!job.bp.nb)
+    return run_pairs(st, job.spectra(ws), job.norms(ws), job.n, job.C, job.P, job.prescale, job.shift, thr, n_hist,
+                     vp, lp, vn, ln, hmax, hmin, stream, job.stype, range_begin, range_end);
+  // the W frames are the j side (TMA-staged columns), the A frames row i
+  return run_pairs(st, job.spectra_w(ws), job.norms(ws), job.n, job.C, job.P, job.prescale, job.shift, thr, n_hist,
+                   vp, lp, vn, ln, hmax, hmin, stream, job.stype, range_begin, range_end, job.spectra(ws),
+                   job.spec_rows());
+}
+
+static PairBandPlan job_band_plan(const FftJob &job, void *ws) {
+  return job.bp.nb ? pair_band_plan(job.P, job.spectra_w(ws), job.stype, job.n, job.C, job.spectra(ws),
+                                    job.spec_rows())
+                   : pair_band_plan(job.P, job.spectra(ws), job.stype, job.n, job.C);
 }
 
 int device_context(int *sm_count, const float2 **twiddles, int **error_flag) {
@@ -319,27 +440,40 @@ int check_xcorr_args(long long n_events, int n_channels, int event_length, int p
 }
 
 // Core: spectra + pairs on `stream`; buffers all on device.
+// stages: 1 = the per-event transforms into ws (spectra + norms, or the
+// lag form's planes + norms), 2 = the pairs from ws, 3 = both.
 static int run_xcorr(const DeviceState &st, const float *d_events, long long n, int C, int L, long long ev_stride,
                      long long ch_stride, int P, int shift, float thr, int n_hist, float *vp, int *lp, float *vn,
-                     int *ln, int *hmax, int *hmin, void *ws, cudaStream_t stream, int form = SEISMIC_FORM_FP32) {
+                     int *ln, int *hmax, int *hmin, void *ws, cudaStream_t stream, int form = SEISMIC_FORM_FP32,
+                     int stages = 3) {
   if (is_lag_form(form)) {
-    int launched = 0;
-    cudaError_t e = launch_lag_gemm(d_events, n, C, L, ev_stride, ch_stride, shift, thr, n_hist, vp, lp, vn, ln,
-                                    hmax, hmin, ws, st.error_flag, st.sm_count, stream, &launched, form);
-    g_launches.fetch_add(launched);
-    SEISMIC_TRY(e, "lag-GEMM launch");
+    if (stages == 3) {
+      int launched = 0;
+      cudaError_t e = launch_lag_gemm(d_events, n, C, L, ev_stride, ch_stride, shift, thr, n_hist, vp, lp, vn, ln,
+                                      hmax, hmin, ws, st.error_flag, st.sm_count, stream, &launched, form);
+      g_launches.fetch_add(launched);
+      SEISMIC_TRY(e, "lag-GEMM launch");
+      return SEISMIC_OK;
+    }
+    if (stages & 1) {
+      SEISMIC_TRY(lag_prepare(d_events, n, C, L, ev_stride, ch_stride, form, ws, stream), "lag-GEMM prep");
+      g_launches.fetch_add(1);
+    }
+    if (stages & 2) {
+      SEISMIC_TRY(launch_lag_blocks(ws, n, C, L, shift, thr, n_hist, vp, lp, vn, ln, hmax, hmin, st.error_flag,
+                                    st.sm_count, stream, form, 0, lag_blocks(n)),
+                  "lag-GEMM launch");
+      g_launches.fetch_add(1);
+    }
     return SEISMIC_OK;
   }
-  const long long rows = n * C;
-  const int stype = form_stype(form);
-  void *spectra = ws;
-  double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(ws) + spectra_bytes(rows, P, stype));
-  // half-precision spectra are always scaled by 1/norm (keeps |X| <= sqrt(L))
-  const int prescale = (C > 1 || stype != 0) ? 1 : 0;
-  int s = run_spectra(st, d_events, n, C, L, ev_stride, ch_stride, P, prescale, spectra, norms, stream, stype);
-  if (s) return s;
-  return run_pairs(st, spectra, norms, n, C, P, prescale, shift, thr, n_hist, vp, lp, vn, ln, hmax, hmin, stream,
-                   stype);
+  const FftJob job = fft_job(n, C, L, shift, P, form_stype(form));
+  if (stages & 1) {
+    const int s = run_fft_spectra(st, job, d_events, ev_stride, ch_stride, ws, stream);
+    if (s) return s;
+  }
+  if (stages & 2) return run_fft_pairs(st, job, ws, thr, n_hist, vp, lp, vn, ln, hmax, hmin, stream);
+  return SEISMIC_OK;
 }
 
 }  // namespace seismic
@@ -384,8 +518,21 @@ size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int eve
   }
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
   if (!supported_padded_size(padded_size)) return 0;
-  const long long rows = n_events * n_channels;
-  return spectra_bytes(rows, padded_size, form_stype(form)) + norms_bytes(rows);
+  return fft_job(n_events, n_channels, event_length, shift, padded_size, form_stype(form)).total();
+}
+
+int seismic_fft_plan(int event_length, int shift, int padded_size, int n_channels, int form, int *transform_size,
+                     int *blocks, int *block_length) {
+  set_status(SEISMIC_OK, "");
+  if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  int s = validate(1, n_channels, event_length, padded_size, shift, 0, form);
+  if (s) return s;
+  if (is_lag_form(form)) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "lag-GEMM forms use no transform");
+  const BlockPlan bp = block_plan(event_length, shift, padded_size, n_channels, form_stype(form));
+  if (transform_size) *transform_size = bp.nb ? bp.Q : padded_size;
+  if (blocks) *blocks = bp.nb;
+  if (block_length) *block_length = bp.nb ? bp.B : event_length;
+  return SEISMIC_OK;
 }
 
 int seismic_check_device_error(void) {
@@ -410,7 +557,21 @@ int seismic_xcorr_device(const float *d_events, long long n_events, int n_channe
                          float threshold, int n_classes_hist, int form, float *d_vals_pos, int *d_lags_pos,
                          float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist, void *workspace,
                          size_t workspace_bytes, void *stream) {
+  return seismic_xcorr_device_stages(d_events, n_events, n_channels, event_length, event_stride, channel_stride,
+                                     padded_size, shift, threshold, n_classes_hist, form, d_vals_pos, d_lags_pos,
+                                     d_vals_neg, d_lags_neg, d_max_hist, d_min_hist, workspace, workspace_bytes,
+                                     stream, 3);
+}
+
+int seismic_xcorr_device_stages(const float *d_events, long long n_events, int n_channels, int event_length,
+                                long long event_stride, long long channel_stride, int padded_size, int shift,
+                                float threshold, int n_classes_hist, int form, float *d_vals_pos, int *d_lags_pos,
+                                float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist,
+                                void *workspace, size_t workspace_bytes, void *stream, int stages) {
   set_status(SEISMIC_OK, "");
+  if (stages < 1 || stages > 3) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "stages must be 1, 2 or 3");
+  if (stages != 3 && !workspace)
+    return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "running one stage needs the caller's workspace");
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
   int s = validate(n_events, n_channels, event_length, padded_size, shift, n_classes_hist, form);
   if (s) return s;
@@ -434,7 +595,7 @@ int seismic_xcorr_device(const float *d_events, long long n_events, int n_channe
   }
   return run_xcorr(*st, d_events, n_events, n_channels, event_length, event_stride, channel_stride, padded_size,
                    shift, threshold, n_classes_hist, d_vals_pos, d_lags_pos, d_vals_neg, d_lags_neg, d_max_hist,
-                   d_min_hist, workspace, (cudaStream_t)stream, form);
+                   d_min_hist, workspace, (cudaStream_t)stream, form, stages);
 }
 
 int seismic_spectra_device(const float *d_events, long long n_events, int n_channels, int event_length,
@@ -611,16 +772,10 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
     // FFT forms: the pair kernels walk the triangle in L2 row bands, whose
     // outputs are contiguous packed rows: launch them in chunks of bands
     // and copy each chunk back on a second stream while the next one runs
-    const long long rows_total = n_events * n_channels;
-    const int stype = form_stype(form);
-    const int prescale = (n_channels > 1 || stype != 0) ? 1 : 0;
-    void *spectra = d_ws;
-    double *norms = reinterpret_cast<double *>(reinterpret_cast<char *>(d_ws) + spectra_bytes(rows_total, padded_size,
-                                                                                            stype));
-    s = run_spectra(*st, d_ev, n_events, n_channels, event_length, (long long)n_channels * event_length, event_length,
-                    padded_size, prescale, spectra, norms, stream, stype);
+    const FftJob job = fft_job(n_events, n_channels, event_length, shift, padded_size, form_stype(form));
+    s = run_fft_spectra(*st, job, d_ev, (long long)n_channels * event_length, event_length, d_ws, stream);
     if (s) return s;
-    const PairBandPlan bp = pair_band_plan(padded_size, spectra, stype, n_events, n_channels);
+    const PairBandPlan bp = job_band_plan(job, d_ws);
     const long long bands = band_count(bp.nb, bp.band);
     const int chunks = (int)(bands < kHostChunks ? bands : kHostChunks);
     if (!st->copy_stream)
@@ -636,10 +791,9 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
       if (k == chunks - 1) k1 = bands;
       const long long r0 = band_row(bp, k0, n_events), r1 = band_row(bp, k1, n_events);
       const long long p0 = packed_row_start(r0, n_events), p1 = packed_row_start(r1, n_events);
-      s = run_pairs(*st, spectra, norms, n_events, n_channels, padded_size, prescale, shift, threshold,
-                    n_classes_hist, d_vp, d_lp, d_vn, d_ln, d_hmax, d_hmin, stream, stype,
-                    band_first_tile(k0, bp.nb, bp.band) * bp.items_per_tile,
-                    band_first_tile(k1, bp.nb, bp.band) * bp.items_per_tile);
+      s = run_fft_pairs(*st, job, d_ws, threshold, n_classes_hist, d_vp, d_lp, d_vn, d_ln, d_hmax, d_hmin, stream,
+                        band_first_tile(k0, bp.nb, bp.band) * bp.items_per_tile,
+                        band_first_tile(k1, bp.nb, bp.band) * bp.items_per_tile);
       if (s) {
         status = s;
         break;

@@ -29,7 +29,31 @@ struct SpectraArgs {
   double *norms;           // out [n_events*n_channels], FP64 L2 norms
   float2 *inv_norms;       // out [n_events*n_channels], FP64 1/norm as hi + lo floats (0 for 0)
   const float2 *twiddles;  // twiddle_table()
+  // Overlap-save frames (blocks > 0, block_spectra_kernel): per (event,
+  // channel) row, `blocks` pairs of size-P transforms.  Frame b covers
+  // samples o_b .. o_b + P - 1, o_b = b * block_len - block_shift; the A
+  // frame keeps samples b * block_len .. + block_len - 1 (zero elsewhere),
+  // the W frame all of them.  A spectra go to `spectra`, W spectra to
+  // `spectra_w`, both [n_events*n_channels][blocks][P/2].
+  int blocks;
+  int block_len;
+  int block_shift;
+  void *spectra_w;
 };
+
+// Overlap-save plan of a short lag window (block_plan, api.cu): the
+// correlation at lags 1-shift .. shift of events of L samples is the sum
+// over nb blocks of B samples of size-Q circular correlations of an A frame
+// (the block) with a W frame (the block widened by `shift` on both sides),
+// exact while B + 2 shift <= Q; the Q-point transforms then replace the
+// size-P one.  nb == 0: no plan (the plain size-P form).
+struct BlockPlan {
+  int Q = 0;       // frame (FFT) size
+  int B = 0;       // block length
+  int nb = 0;      // blocks per (event, channel) row
+};
+BlockPlan block_plan(int length, int shift, int P, int n_channels, int stype);
+cudaError_t launch_block_spectra(int Q, const SpectraArgs &a, cudaStream_t s);
 
 // A norms buffer holds `rows` FP64 norms followed by `rows` inverse norms
 // 1/norm, each computed in FP64 and stored as an unevaluated float pair
@@ -92,12 +116,22 @@ struct PairArgs {
   int band_tiles;
   int ring;
   int *error_flag;
+  // Overlap-save form (staged form only): i-side spectra that differ from the
+  // j-side ones (the A frames; `spectra` holds the W frames), and spectrum
+  // rows per event (n_channels * blocks; 0 = n_channels).
+  const void *spectra_i;
+  int spec_channels;
   // Poll limit of the staged form's producer waits (0: the built-in limit,
   // seconds of back-off).  Set from SEISMIC_DEVICE_WAIT_POLLS: a few polls
   // make the waits run out on a healthy GPU, which is how the abort path and
   // its error status are tested.
   unsigned wait_limit;
 };
+
+// Spectrum rows per event of the pair launch `a` (channels x blocks).
+__host__ __device__ inline int spectrum_rows(const PairArgs &a) {
+  return a.spec_channels > 0 ? a.spec_channels : a.n_channels;
+}
 
 // SEISMIC_DEVICE_WAIT_POLLS (1 .. 2^30), else 0.
 inline unsigned device_wait_polls() {
@@ -137,6 +171,9 @@ __host__ __device__ __forceinline__ long long band_first_tile(long long k, long 
 // ---- staged pair form (pairs_staged.cu): spectra staged into shared memory
 // by TMA (P = 4096 by default).  Work items are (event i, T consecutive j).
 bool staged_supported(int P, const PairArgs &a);
+// The staged form can run at all (not disabled by SEISMIC_PAIR_KERNEL=direct,
+// and the driver's tensor-map encoder is available).
+bool staged_enabled();
 long long staged_items_total(int P, const PairArgs &a);  // triangle or rectangle
 int staged_tile_side(int P, const PairArgs &a);         // T: events per tile side (items per tile)
 // Launches items [a.couple_begin, a.couple_end) of the staged decomposition.

@@ -152,8 +152,8 @@ __device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMa
   using ST_T = typename SpecT<ST>::T;
   constexpr int S = SH::S, H = P / 2;
   constexpr uint32_t CHUNK = (uint32_t)(S * sizeof(ST_T));
-  const int C = a.n_channels;
-  const ST_T *spec_i = reinterpret_cast<const ST_T *>(a.rect ? a.spectra_q : a.spectra);
+  const int C = spectrum_rows(a);
+  const ST_T *spec_i = reinterpret_cast<const ST_T *>(a.spectra_i ? a.spectra_i : (a.rect ? a.spectra_q : a.spectra));
   const long long n_i = a.rect ? a.n_query : a.n_events;
   const long long i = cur->i < n_i ? cur->i : n_i - 1;  // ragged last tile row: staged but unused
   const int c = cur->c, r = cur->r;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
   uint64_t *empty = full + K;
   int *hist = reinterpret_cast<int *>(empty + K);
   const bool smem_hist = a.n_hist > 0 && a.n_hist <= kStagedHistMax;
-  const int C = a.n_channels;
+  const int C = spectrum_rows(a);  // spectrum rows per event: channels, times blocks in the overlap-save form
   const long long N = a.n_events;
 
   if (threadIdx.x == 0) {
@@ -363,15 +363,18 @@ static int staged_ru() {
 // (measured, staged vs direct M pairs/s: P=512 C=1 973 vs 926, P=1024 C=1
 // 549 vs 496, C=3 379 vs 339).  SEISMIC_PAIR_KERNEL=direct forces the direct
 // form everywhere.
+bool staged_enabled() { return !staged_disabled() && tensor_map_encoder() != nullptr; }
+
 bool staged_supported(int P, const PairArgs &a) {
   if (P < 512 || P > 4096 || staged_disabled()) return false;
   if (a.stype < 0 || a.stype > 2) return false;
   if ((reinterpret_cast<uintptr_t>(a.spectra) & 15u) != 0) return false;
   if (a.rect && (reinterpret_cast<uintptr_t>(a.spectra_q) & 15u) != 0) return false;
+  if (a.spectra_i && (reinterpret_cast<uintptr_t>(a.spectra_i) & 15u) != 0) return false;
   return tensor_map_encoder() != nullptr;
 }
 
-int staged_tile_side(int P, const PairArgs &a) { return 2 * (staged_nwarp(P, a.stype, a.n_channels) * 32 / (P / 32)); }
+int staged_tile_side(int P, const PairArgs &a) { return 2 * (staged_nwarp(P, a.stype, spectrum_rows(a)) * 32 / (P / 32)); }
 
 long long staged_items_total(int P, const PairArgs &a) {
   const long long T = staged_tile_side(P, a);
@@ -397,15 +400,15 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
     cudaError_t e = ensure_dynamic_smem((const void *)staged_pair_kernel<P, NWARP, RU, ST>, (int)kStagedSmemBudget);
     if (e != cudaSuccess) return e;
   }
-  a.band_tiles = l2_band_tiles(a.n_channels, P, (int)sizeof(ST_T), SH::T);
+  a.band_tiles = l2_band_tiles(spectrum_rows(a), P, (int)sizeof(ST_T), SH::T);
   a.wait_limit = device_wait_polls();
 
   // Tensor map of the j spectra: dims {P/2 bins, C channels, N events},
   // box {S bins, 1 channel, T events}.
   CUtensorMap map;
-  const cuuint64_t dims[3] = {(cuuint64_t)(P / 2), (cuuint64_t)a.n_channels, (cuuint64_t)a.n_events};
+  const cuuint64_t dims[3] = {(cuuint64_t)(P / 2), (cuuint64_t)spectrum_rows(a), (cuuint64_t)a.n_events};
   const cuuint64_t strides[2] = {(cuuint64_t)(P / 2) * sizeof(ST_T),
-                                 (cuuint64_t)a.n_channels * (P / 2) * sizeof(ST_T)};
+                                 (cuuint64_t)spectrum_rows(a) * (P / 2) * sizeof(ST_T)};
   const cuuint32_t box[3] = {(cuuint32_t)SH::S, 1u, (cuuint32_t)SH::T};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt = sizeof(ST_T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
@@ -424,15 +427,15 @@ template <int P> static cudaError_t launch_staged_p(const PairArgs &a, int sm_co
   switch (a.stype) {
     case 0:
       // the wide CTA's exchange buffers leave room for a ring of 2-chunk slots
-      if (staged_nwarp(P, 0, a.n_channels) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 2, 0>(a, sm_count, s);
+      if (staged_nwarp(P, 0, spectrum_rows(a)) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 2, 0>(a, sm_count, s);
       return staged_ru() == 2 ? launch_staged_t<P, kStagedWarps, 2, 0>(a, sm_count, s)
                               : launch_staged_t<P, kStagedWarps, 4, 0>(a, sm_count, s);
     // half-precision spectra: half the ring bytes, so the wide CTA keeps 4-chunk slots
     case 1:
-      if (staged_nwarp(P, 1, a.n_channels) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 4, 1>(a, sm_count, s);
+      if (staged_nwarp(P, 1, spectrum_rows(a)) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 4, 1>(a, sm_count, s);
       return launch_staged_t<P, kStagedWarps, 4, 1>(a, sm_count, s);
     case 2:
-      if (staged_nwarp(P, 2, a.n_channels) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 4, 2>(a, sm_count, s);
+      if (staged_nwarp(P, 2, spectrum_rows(a)) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 4, 2>(a, sm_count, s);
       return launch_staged_t<P, kStagedWarps, 4, 2>(a, sm_count, s);
     default: return cudaErrorInvalidValue;
   }

@@ -305,4 +305,137 @@ cudaError_t launch_spectra(int P, const SpectraArgs &a, cudaStream_t s) {
 
 bool supported_padded_size(int P) { return P >= kMinP && P <= kMaxP && (P & (P - 1)) == 0; }
 
+// ------------------------------------------------------- overlap-save frames
+// One group of G = Q/32 threads per (event, channel) row: the row's FP64
+// norm over its L samples (the same float-pair energy as spectra_body), then
+// for every block b one complex size-Q FFT whose real part is the A frame
+// and imaginary part the W frame, split as in spectra_body.  Both spectra
+// carry the row's 1/norm when prescale is set.
+template <int Q>
+__global__ void __launch_bounds__(256) block_spectra_kernel(SpectraArgs a) {
+  constexpr int G = Q / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  constexpr int S = Q / 16;
+  constexpr int H = Q / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *bufs = reinterpret_cast<float2 *>(smem_raw);
+  double *reds = reinterpret_cast<double *>(bufs + NG * padded_len<Q>());
+  const int g = threadIdx.x / G;
+  const int t = threadIdx.x % G;
+  float2 *buf = bufs + g * padded_len<Q>();
+  double *red = reds + g * 2 * ((G + 31) / 32);
+  const long long rows = a.n_events * (long long)a.n_channels;
+  const long long row = (long long)blockIdx.x * NG + g;
+  if (row >= rows) return;  // whole group leaves together
+  const float *src = a.events + (row / a.n_channels) * a.ev_stride + (row % a.n_channels) * a.ch_stride;
+  const int L = a.length;
+
+  // ---- norm over the L samples
+  float m = 0.f;
+  for (int s = t; s < L; s += G) m = fmaxf(m, fabsf(__ldg(src + s)));
+  const int xe = energy_exponent(group_max_float<G>(m, red, g, t));
+  const EnergyScale sc(xe);
+  float eh = 0.f, el = 0.f;
+  for (int s = t; s < L; s += G) add_square(sc(__ldg(src + s)), eh, el);
+  group_sum_pair<G>(eh, el, red, g, t);
+  if (t == 0) {
+    const double nrm = sqrt(ldexp((double)eh + (double)el, 2 * xe));
+    const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    a.norms[row] = nrm;
+    a.inv_norms[row] = split_double(inv);
+    reinterpret_cast<float *>(red)[0] = a.prescale ? (float)inv : 1.f;
+  }
+  group_sync<G>(g);
+  const float scale = reinterpret_cast<const float *>(red)[0];
+
+  using PL = FftPlan<Q>;
+  for (int b = 0; b < a.blocks; ++b) {
+    const int o = b * a.block_len - a.block_shift;  // frame origin in the row
+    float2 v[32];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int c = t + half * (S / 2);
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const int k = c + r * S;  // frame index
+        const int n = o + k;      // sample index
+        const float x = (n >= 0 && n < L) ? __ldg(src + n) : 0.f;
+        const bool in_a = k >= a.block_shift && k < a.block_shift + a.block_len;
+        v[half * 16 + r] = make_float2(in_a ? x : 0.f, x);
+      }
+    }
+    group_sync<G>(g);  // the previous block's split has read buf
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      dft<16, -1>(&v[half * 16]);
+      const int c = t + half * (S / 2);
+#pragma unroll
+      for (int r = 0; r < 16; ++r) buf[pad16(c * 16 + r)] = v[half * 16 + r];
+    }
+    group_sync<G>(g);
+    pass_read<Q, PL::R2>(buf, v, t);
+    group_sync<G>(g);
+    pass_compute<Q, PL::R2, 16, -1>(v, t, a.twiddles);
+    pass_write<Q, PL::R2, 16>(buf, v, t);
+    group_sync<G>(g);
+    if constexpr (PL::R3 != 0) {
+      pass_read<Q, PL::R3>(buf, v, t);
+      group_sync<G>(g);
+      pass_compute<Q, PL::R3, 16 * PL::R2, -1>(v, t, a.twiddles);
+      pass_write<Q, PL::R3, 16 * PL::R2>(buf, v, t);
+      group_sync<G>(g);
+    }
+    if constexpr (PL::R4 != 0) {
+      pass_read<Q, PL::R4>(buf, v, t);
+      group_sync<G>(g);
+      pass_compute<Q, PL::R4, 16 * PL::R2 * PL::R3, -1>(v, t, a.twiddles);
+      pass_write<Q, PL::R4, 16 * PL::R2 * PL::R3>(buf, v, t);
+      group_sync<G>(g);
+    }
+    const long long off = (row * a.blocks + b) * (long long)H;
+#pragma unroll 4
+    for (int k = t; k < H; k += G) {
+      const float2 zk = buf[pad16(k)];
+      float2 va, vw;
+      if (k == 0) {
+        const float2 zh = buf[pad16(H)];
+        va = make_float2(zk.x * scale, zh.x * scale);
+        vw = make_float2(zk.y * scale, zh.y * scale);
+      } else {
+        const float2 zm = buf[pad16(Q - k)];
+        const float2 A = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+        const float2 W = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+        va = make_float2(A.x * scale, A.y * scale);
+        vw = make_float2(W.x * scale, W.y * scale);
+      }
+      store_spectrum(a.spectra, a.stype, off + k, va);
+      store_spectrum(a.spectra_w, a.stype, off + k, vw);
+    }
+  }
+}
+
+template <int Q> static cudaError_t launch_block_spectra_t(const SpectraArgs &a, cudaStream_t s) {
+  constexpr int G = Q / 32;
+  constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
+  const long long rows = a.n_events * (long long)a.n_channels;
+  const long long ctas = (rows + NG - 1) / NG;
+  if (ctas <= 0) return cudaSuccess;
+  if (ctas > 0x7fffffffLL || a.blocks < 1) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)NG * padded_len<Q>() * sizeof(float2) + (size_t)NG * 2 * ((G + 31) / 32) * sizeof(double);
+  cudaError_t e = ensure_dynamic_smem((const void *)block_spectra_kernel<Q>, (int)smem);
+  if (e != cudaSuccess) return e;
+  block_spectra_kernel<Q><<<(unsigned)ctas, NG * G, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_block_spectra(int Q, const SpectraArgs &a, cudaStream_t s) {
+  switch (Q) {
+    case 512: return launch_block_spectra_t<512>(a, s);
+    case 1024: return launch_block_spectra_t<1024>(a, s);
+    case 2048: return launch_block_spectra_t<2048>(a, s);
+    case 4096: return launch_block_spectra_t<4096>(a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 }  // namespace seismic

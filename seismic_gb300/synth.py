@@ -127,3 +127,44 @@ def make_workload(name: str, n_events: int | None = None) -> tuple[np.ndarray, i
         ev = family_catalog(n, w["n_channels"], w["length"],
                             n_families=max(1, min(w["n_families"], n // 32 or 1)), seed=w["seed"])
     return ev, w["shift"]
+
+
+def _family_job(job):
+    n, c, length, seed = job
+    return family_catalog(n, c, length, n_families=max(1, n // 32), seed=seed)
+
+
+def _pool_map(jobs):
+    """family_catalog over jobs in a spawn-context process pool (each job has
+    its own seed, so the result does not depend on the pool)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import os
+    workers = max(1, min(16, len(os.sched_getaffinity(0)), len(jobs)))
+    if workers == 1:
+        return [_family_job(j) for j in jobs]
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_family_job, jobs, chunksize=4))
+
+
+def batched_catalogs(n_catalogs: int = 256, seed: int = 4000) -> list[tuple[np.ndarray, int]]:
+    """The batched workload: independent catalogs with N log-uniform in
+    16..2048, L from {256, 512, 1000, 2048, 3000, 4096}, 1 or 3 channels,
+    families = max(1, N // 32), full lag range (shift = L).  Returns
+    [(events (N, C, L), shift)]."""
+    rng = np.random.default_rng(seed)
+    lengths = [256, 512, 1000, 2048, 3000, 4096]
+    jobs = []
+    for k in range(n_catalogs):
+        n = int(round(np.exp(rng.uniform(np.log(16), np.log(2048)))))
+        length = int(rng.choice(lengths))
+        c = int(rng.choice([1, 3]))
+        jobs.append((n, c, length, seed + 1 + k))
+    return [(ev, job[2]) for ev, job in zip(_pool_map(jobs), jobs)]
+
+
+def serving_catalog(n_events: int = 50000, seed: int = 9000) -> np.ndarray:
+    """The serving workload's resident catalog: family events of 3 channels
+    x 1024 samples, generated in blocks of 2500 (block b seeded seed + b)."""
+    jobs = [(min(2500, n_events - b), 3, 1024, seed + b) for b in range(0, n_events, 2500)]
+    return np.concatenate(_pool_map(jobs))

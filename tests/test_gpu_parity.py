@@ -276,7 +276,8 @@ def test_precision_workload_size_properties(cuda_ok):
 def test_spectra_norms_fp64_over_amplitude_range(cuda_ok, length):
     """Kernel (a)'s norms against numpy FP64 sums of squares, for rows from
     1e-30 to 1e30 in amplitude, a row with one large spike, and a zero row:
-    relative error at the FP64 level, inverse norms rounded once."""
+    relative error at the FP64 level; the inverse norms, kept as hi + lo
+    floats, equal the FP64 inverse to 2^-46 relative with hi rounded once."""
     import torch
     from seismic_gb300 import _lib
     lib = _lib.lib()
@@ -293,11 +294,13 @@ def test_spectra_norms_fp64_over_amplitude_range(cuda_ok, length):
                                           norms.data_ptr(), None))
     torch.cuda.synchronize()
     got = norms[:n].cpu().numpy()
-    inv = norms[n:].cpu().numpy().view(np.float32)[:n]
+    pair = norms[n:].cpu().numpy().view(np.float32).reshape(n, 2)
     want = np.sqrt((ev.astype(np.float64) ** 2).sum(axis=1))
     np.testing.assert_allclose(got[:-1], want[:-1], rtol=1e-12)
-    assert got[-1] == 0.0 and inv[-1] == 0.0
-    np.testing.assert_array_equal(inv[:-1], (1.0 / got[:-1]).astype(np.float32))
+    assert got[-1] == 0.0 and pair[-1, 0] == 0.0 and pair[-1, 1] == 0.0
+    np.testing.assert_array_equal(pair[:-1, 0], (1.0 / got[:-1]).astype(np.float32))
+    inv = pair[:, 0].astype(np.float64) + pair[:, 1].astype(np.float64)
+    np.testing.assert_allclose(inv[:-1], 1.0 / got[:-1], rtol=2.0 ** -46)
 
 
 @pytest.mark.parametrize("n,c,length,shift,form", [(600, 3, 1024, 1024, "fp32"),   # staged form, P=2048
