@@ -275,6 +275,9 @@ typedef struct seismic_catalog {
 typedef struct seismic_batch seismic_batch; /* opaque plan */
 
 #define SEISMIC_BATCH_NO_GRAPH 1 /* flag: launch directly instead of replaying a graph */
+/* flag: one persistent pair launch per transform size on parallel graph
+ * branches, instead of the default single launch over all sizes */
+#define SEISMIC_BATCH_PER_SIZE 2
 
 /* Plans the batch (work lists sorted by cost, tuned tile sizes from the
  * autotuner cache), allocates its workspace and captures the CUDA graph.

@@ -19,6 +19,7 @@ class CCatalog(ctypes.Structure):
 
 
 NO_GRAPH = 1
+PER_SIZE = 2  # one persistent pair launch per transform size instead of one over all sizes
 
 
 def _declare(lib):
@@ -59,7 +60,7 @@ class Batch:
     """Plan + outputs for a list of catalogs (float32 CUDA tensors (N, C, L)
     or (N, L)); run() replays the captured graph on a stream."""
 
-    def __init__(self, events, shifts, thresholds=None, n_classes_hist=0, use_graph=True):
+    def __init__(self, events, shifts, thresholds=None, n_classes_hist=0, use_graph=True, per_size=False):
         import torch
         self.lib = _declare(_lib.lib())
         self.events = [e.contiguous() if e.dim() == 3 else e.contiguous()[:, None, :] for e in events]
@@ -85,7 +86,8 @@ class Batch:
                               o.min_hist.data_ptr() if n_classes_hist else None)
         self._arr = arr
         h = ctypes.c_void_p()
-        _lib.check(self.lib.seismic_batch_create(arr, n, 0 if use_graph else NO_GRAPH, ctypes.byref(h)))
+        flags = (0 if use_graph else NO_GRAPH) | (PER_SIZE if per_size else 0)
+        _lib.check(self.lib.seismic_batch_create(arr, n, flags, ctypes.byref(h)))
         self.handle = h
         self.pairs = int(self.lib.seismic_batch_pairs(h))
         self.kernels_per_run = int(self.lib.seismic_batch_kernels_per_run(h))

@@ -141,7 +141,9 @@ BlockPlan block_plan(int length, int shift, int P, int n_channels, int stype) {
   BlockPlan best;
   const char *env = getenv("SEISMIC_BLOCK_FORM");
   if ((env && strcmp(env, "off") == 0) || !staged_enabled()) return best;
-  if (stype < 0 || stype > 2 || shift < 1 || (long long)length + shift > P) return best;
+  // FP32 and FP16 spectra (BF16's 8-bit mantissa, summed over the frames,
+  // would pass its 1e-3 coefficient bar)
+  if (stype < 0 || stype > 1 || shift < 1 || (long long)length + shift > P) return best;
   auto cost = [&](int q, int nb) {
     return 2.5 * q * (31 - __builtin_clz((unsigned)q)) + 6.0 * n_channels * nb * (q / 2);
   };

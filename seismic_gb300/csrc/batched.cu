@@ -9,13 +9,14 @@
 //    spectra and FP64 norms, and a BatchCatalog descriptor in device memory;
 //  * spectra work: one item per CTA's worth of row pairs (NG(P) of them),
 //    all catalogs in one launch (batched_spectra_kernel switches on P);
-//  * pair work, per transform size P present: items of item_groups * NG(P)
-//    couples, sorted by decreasing cost (couples * (P log2 P + products)),
-//    handed out by an atomic counter to a persistent batched_pair_kernel<P>
-//    (one template instance per size keeps each at the single-catalog
-//    kernel's register budget);
-//  * the graph: counters reset -> spectra -> fork into one branch per size
-//    (largest total work first) -> join.
+//  * pair work: items of item_groups * NG(P) couples of every catalog, all
+//    sizes in one list sorted by decreasing cost (couples * (P log2 P +
+//    products)), handed out by an atomic counter to ONE persistent launch of
+//    batched_pair_kernel_mixed, which switches on each item's P;
+//  * the graph: counter reset -> spectra -> pairs (two kernels per run).
+//  * With SEISMIC_BATCH_PER_SIZE (flag), the pair work runs instead as one
+//    persistent batched_pair_kernel<P> per size present, on fork/join
+//    branches of the graph (largest total work first).
 // seismic_batch_run only replays the graph: one host call, no allocation.
 #include <algorithm>
 #include <cmath>
@@ -41,6 +42,9 @@ struct SizeClass {
 struct seismic_batch {
   int device = 0;
   bool use_graph = true;
+  bool per_size = false;   // one pair launch per transform size instead of one mixed launch
+  long long n_pair_items = 0;
+  int mixed_grid = 0;
   seismic::BatchCatalog *d_cats = nullptr;
   seismic::BatchItem *d_spec_items = nullptr;
   seismic::BatchItem *d_pair_items = nullptr;
@@ -62,6 +66,12 @@ namespace {
 int enqueue(seismic_batch *b, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned long long) * b->classes.size(), s);
   if (e == cudaSuccess) e = launch_batched_spectra(b->d_cats, b->d_spec_items, b->n_spec_items, b->spec_grid, s);
+  if (!b->per_size) {
+    if (e == cudaSuccess)
+      e = launch_batched_pairs_mixed(b->d_cats, b->d_pair_items, b->n_pair_items, b->d_counters, b->mixed_grid,
+                                     b->max_hist, s);
+    return e == cudaSuccess ? SEISMIC_OK : report_cuda(e, "batched launch");
+  }
   if (e == cudaSuccess) e = cudaEventRecord(b->fork, s);
   for (size_t k = 0; e == cudaSuccess && k < b->classes.size(); ++k) {
     SizeClass &c = b->classes[k];
@@ -134,6 +144,7 @@ extern "C" int seismic_batch_create(const seismic_catalog *catalogs, int n_catal
 
   seismic_batch *b = new seismic_batch();
   b->use_graph = !(flags & SEISMIC_BATCH_NO_GRAPH);
+  b->per_size = (flags & SEISMIC_BATCH_PER_SIZE) != 0;
   b->total_pairs = total_pairs;
   b->max_hist = max_hist;
   cudaGetDevice(&b->device);
@@ -206,6 +217,18 @@ extern "C" int seismic_batch_create(const seismic_catalog *catalogs, int n_catal
 
   // per size: items largest first; sizes ordered by total work (largest first)
   std::vector<BatchItem> pair_items;
+  if (!b->per_size) {  // one list over every size, largest first, one counter
+    std::vector<std::pair<double, BatchItem>> all;
+    for (auto &kv : by_size) all.insert(all.end(), kv.second.begin(), kv.second.end());
+    std::stable_sort(all.begin(), all.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
+    for (auto &it : all) pair_items.push_back(it.second);
+    SizeClass sc;  // one class: the counter and the item count
+    sc.n_items = (long long)pair_items.size();
+    b->classes.push_back(sc);
+    b->n_pair_items = (long long)pair_items.size();
+    b->mixed_grid = sm_count * batched_mixed_ctas_per_sm(max_hist);  // also sets the kernel attribute
+    by_size.clear();
+  }
   for (auto &kv : by_size) {
     auto &v = kv.second;
     std::stable_sort(v.begin(), v.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
@@ -238,6 +261,7 @@ extern "C" int seismic_batch_create(const seismic_catalog *catalogs, int n_catal
                    cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   for (auto &c : b->classes) {
+    if (!b->per_size) break;  // branches only for per-size launches
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.branch, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming);
   }
@@ -288,7 +312,7 @@ extern "C" int seismic_batch_run(seismic_batch *b, void *stream) {
     const int st = enqueue(b, s);
     if (st) return st;
   }
-  note_launches(1 + (unsigned)b->classes.size());
+  note_launches((unsigned)seismic_batch_kernels_per_run(b));
   return SEISMIC_OK;
 }
 
@@ -300,5 +324,6 @@ extern "C" int seismic_batch_destroy(seismic_batch *b) {
 
 extern "C" long long seismic_batch_pairs(const seismic_batch *b) { return b ? b->total_pairs : 0; }
 extern "C" int seismic_batch_kernels_per_run(const seismic_batch *b) {
-  return b ? 1 + (int)b->classes.size() : 0;
+  if (!b) return 0;
+  return b->per_size ? 1 + (int)b->classes.size() : 2;
 }

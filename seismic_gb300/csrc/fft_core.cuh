@@ -219,6 +219,25 @@ template <int G> __device__ __forceinline__ void group_sync(int group_in_cta) {
   }
 }
 
+// group_sync that also returns, on every thread of the group, whether `v`
+// is set on any of them (a warp vote, or a named-barrier OR-reduction for
+// groups wider than a warp, which is a barrier like bar.sync).
+template <int G> __device__ __forceinline__ bool group_sync_any(int group_in_cta, bool v) {
+  if constexpr (G <= 32) {
+    __syncwarp(group_lane_mask<G>());
+    return __any_sync(group_lane_mask<G>(), v);
+  } else {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.or.pred po, %2, %3, pi;\n"
+        " selp.u32 %0, 1, 0, po;\n}"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(group_in_cta + 1), "r"(G)
+        : "memory");
+    return r != 0;
+  }
+}
+
 // Stockham pass helpers for passes after the first.  A pass of radix R has
 // P/R butterflies ("jobs"); thread t of the group runs jobs t + q*G,
 // q = 0..32/R-1, holding them in v[q*R + r].

@@ -58,7 +58,8 @@ cudaError_t launch_block_spectra(int Q, const SpectraArgs &a, cudaStream_t s);
 // A norms buffer holds `rows` FP64 norms followed by `rows` inverse norms
 // 1/norm, each computed in FP64 and stored as an unevaluated float pair
 // hi + lo (hi = the float nearest to it, lo = the float nearest to the
-// rest): 48 significant bits, from which the final normalisation of every
+// rest): 48 significant bits (fewer for norms above ~2^102, whose lo part
+// falls into FP32's subnormal range), from which the final normalisation of every
 // form is computed at FP64-equivalent accuracy without FP64 instructions in
 // the FFT pair loop (compensated_scale below).
 inline size_t norms_buffer_bytes(long long rows) { return ((size_t)rows * 16 + 255) / 256 * 256; }
@@ -220,6 +221,10 @@ cudaError_t launch_batched_pairs(int P, const BatchCatalog *cats, const BatchIte
                                  unsigned long long *counter, int grid, int max_hist, cudaStream_t s);
 // Also sets the kernel's shared-memory attribute: call before any capture.
 int batched_pairs_ctas_per_sm(int P, int max_hist);
+// One persistent launch over the items of every size (batched_pair_kernel_mixed).
+cudaError_t launch_batched_pairs_mixed(const BatchCatalog *cats, const BatchItem *items, long long n_items,
+                                       unsigned long long *counter, int grid, int max_hist, cudaStream_t s);
+int batched_mixed_ctas_per_sm(int max_hist);  // sets the attribute too: before any capture
 int groups_per_cta(int P);  // 256 / (P / 32), at least 1
 
 // Device context for entry points in other translation units (api.cu).

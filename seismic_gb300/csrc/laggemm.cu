@@ -186,8 +186,11 @@ static LagSmem lag_smem_layout(const LagArgs &a) {
 constexpr uint32_t kLagWaitPolls = 1u << 22;
 
 // Bounded wait.  The CTA's poll limit (LagArgs::wait_limit, or the default)
-// is the shared word right after its abort flag.
+// is the shared word right after its abort flag, read only when the barrier
+// is not complete at the first poll (the MMA warp's waits sit on its issue
+// path).
 __device__ __forceinline__ bool lag_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err) {
+  if (tc::mbar_try_wait(bar, parity)) return true;
   const uint32_t limit = reinterpret_cast<const volatile uint32_t *>(abort_flag)[1];
   for (uint32_t it = 0; it < limit; ++it) {
     if (tc::mbar_try_wait(bar, parity)) return true;

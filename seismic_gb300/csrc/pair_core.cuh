@@ -207,9 +207,13 @@ __device__ __forceinline__ void assemble_couple(const CoupleAcc &y, int t, float
 // Unnormalised inverse FFT of size P by a group of G = P/32 threads: pass 1
 // (radix 16, no twiddles) on both columns in registers, then the Stockham
 // passes of FftPlan<P> through the group's padded exchange buffer.
+// With `stop` (the staged form's abort), the first group barrier also ORs
+// *stop over the group; if it comes out set, every thread of the group
+// returns there (the caller then leaves its item loop).
 template <int P>
 __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, int t, int g, int ca, int cb,
-                                                  const float2 *__restrict__ tw, const TwiddleRoots<P, 1> &roots) {
+                                                  const float2 *__restrict__ tw, const TwiddleRoots<P, 1> &roots,
+                                                  bool *stop = nullptr) {
   using PL = FftPlan<P>;
   constexpr int G = P / 32;
   dft<16, 1>(&v[0]);
@@ -219,7 +223,12 @@ __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, 
     buf[pad16(ca * 16 + r)] = v[r];
     buf[pad16(cb * 16 + r)] = v[16 + r];
   }
-  group_sync<G>(g);
+  if (stop) {
+    *stop = group_sync_any<G>(g, *stop);
+    if (*stop) return;
+  } else {
+    group_sync<G>(g);
+  }
   pass_read<P, PL::R2>(buf, v, t);
   group_sync<G>(g);
   pass_compute<P, PL::R2, 16, 1>(v, t, tw, roots.template get<2>());

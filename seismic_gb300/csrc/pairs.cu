@@ -17,6 +17,7 @@
 // taking neighbouring couples of the same tile, whose spectra they read
 // straight from global memory (L2).  This form serves every size P and the
 // batched launch; pairs_staged.cu stages the spectra through shared memory.
+#include <algorithm>
 #include "pair_core.cuh"
 
 namespace seismic {
@@ -208,6 +209,45 @@ __global__ void __launch_bounds__(256, 2)
   }
 }
 
+// Persistent over every catalog of a batch whatever its transform size: the
+// item's catalog descriptor names P, and the CTA's 256 threads run that
+// size's groups for the item (every size uses 256 threads x 32 values and
+// the same shared-memory footprint).  One launch covers the whole batch, and
+// the items of all sizes, sorted by cost, balance across the SMs together.
+__global__ void __launch_bounds__(256, 2)
+    batched_pair_kernel_mixed(const BatchCatalog *__restrict__ cats, const BatchItem *__restrict__ items,
+                              long long n_items, unsigned long long *counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long s_item;
+  __shared__ BatchItem s_w;
+  __shared__ int s_p;
+  __shared__ __align__(16) PairArgs s_args;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_item = (long long)atomicAdd(counter, 1ULL);
+      if (s_item < n_items) {
+        s_w = items[s_item];
+        s_args = cats[s_w.cat].pairs;
+        s_p = cats[s_w.cat].P;
+      }
+    }
+    __syncthreads();
+    if (s_item >= n_items) break;
+    switch (s_p) {  // uniform over the CTA
+      case 64: batched_pair_item<64>(s_args, s_w.begin, s_w.end, smem_raw); break;
+      case 128: batched_pair_item<128>(s_args, s_w.begin, s_w.end, smem_raw); break;
+      case 256: batched_pair_item<256>(s_args, s_w.begin, s_w.end, smem_raw); break;
+      case 512: batched_pair_item<512>(s_args, s_w.begin, s_w.end, smem_raw); break;
+      case 1024: batched_pair_item<1024>(s_args, s_w.begin, s_w.end, smem_raw); break;
+      case 2048: batched_pair_item<2048>(s_args, s_w.begin, s_w.end, smem_raw); break;
+      case 4096: batched_pair_item<4096>(s_args, s_w.begin, s_w.end, smem_raw); break;
+      case 8192: batched_pair_item<8192>(s_args, s_w.begin, s_w.end, smem_raw); break;
+      default: break;
+    }
+    __syncthreads();  // s_item and the shared buffers are reused by the next item
+  }
+}
+
 template <int P> static size_t batched_pair_smem_t(int max_hist) {
   constexpr int G = P / 32;
   constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
@@ -232,6 +272,29 @@ static cudaError_t launch_batched_t(const BatchCatalog *cats, const BatchItem *i
   // the shared-memory attribute was set by batched_pairs_ctas_per_sm during planning,
   // so nothing but the launch happens here (it may be inside a stream capture)
   batched_pair_kernel<P><<<grid, 256, batched_pair_smem_t<P>(max_hist), s>>>(cats, items, n_items, counter);
+  return cudaGetLastError();
+}
+
+static size_t batched_mixed_smem(int max_hist) {
+  return std::max({batched_pair_smem_t<64>(max_hist), batched_pair_smem_t<128>(max_hist),
+                   batched_pair_smem_t<256>(max_hist), batched_pair_smem_t<512>(max_hist),
+                   batched_pair_smem_t<1024>(max_hist), batched_pair_smem_t<2048>(max_hist),
+                   batched_pair_smem_t<4096>(max_hist), batched_pair_smem_t<8192>(max_hist)});
+}
+
+int batched_mixed_ctas_per_sm(int max_hist) {
+  int n = 0;
+  ensure_dynamic_smem((const void *)batched_pair_kernel_mixed, (int)batched_mixed_smem(kSmemHistMax));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batched_pair_kernel_mixed, 256,
+                                                    batched_mixed_smem(max_hist)) != cudaSuccess)
+    n = 1;
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_batched_pairs_mixed(const BatchCatalog *cats, const BatchItem *items, long long n_items,
+                                       unsigned long long *counter, int grid, int max_hist, cudaStream_t s) {
+  // attribute set by batched_mixed_ctas_per_sm during planning (no API call here: may be captured)
+  batched_pair_kernel_mixed<<<grid, 256, batched_mixed_smem(max_hist), s>>>(cats, items, n_items, counter);
   return cudaGetLastError();
 }
 

@@ -114,23 +114,6 @@ __device__ __forceinline__ bool consumer_wait(uint64_t *bar, uint32_t parity, vo
   }
 }
 
-// True on every thread of the group if `v` is true on any of them.  All G
-// threads of the group must call it (a warp vote, or a named-barrier
-// reduction for groups wider than a warp).
-template <int G> __device__ __forceinline__ bool group_any(int group_in_cta, bool v) {
-  if constexpr (G <= 32) {
-    return __any_sync(group_lane_mask<G>(), v);
-  } else {
-    uint32_t r;
-    asm volatile(
-        "{\n .reg .pred pi, po;\n setp.ne.u32 pi, %1, 0;\n bar.red.or.pred po, %2, %3, pi;\n"
-        " selp.u32 %0, 1, 0, po;\n}"
-        : "=r"(r)
-        : "r"((uint32_t)v), "r"(group_in_cta + 1), "r"(G)
-        : "memory");
-    return r != 0;
-  }
-}
 
 // Default poll limit of the producer's waits (with back-off: seconds).
 constexpr uint32_t kStagedWaitPolls = 1u << 24;
@@ -308,12 +291,17 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
           }
         }
       }
-      if (group_any<G>(g, stop)) break;  // aborted inside the item: leave together
+      // an abort inside the item: the group leaves together, by the vote
+      // folded into the inverse FFT's first barrier (or a vote of its own
+      // for a group without a pair in this item)
       if (live) {  // uniform over the group
         float2 v[32];
         assemble_couple(y, t, v);
-        inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots);
+        inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots, &stop);
+        if (stop) break;
         scan_and_write<P>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist, wmask);
+      } else if (group_sync_any<G>(g, stop)) {
+        break;
       }
     }
   }

@@ -1,7 +1,9 @@
-"""GPU tests of the batched form (many catalogs, persistent per-size pair
-launches, captured CUDA graph) and of the autotuner.  Each catalog of a
-batch must give exactly what the single-catalog FP32 path gives at the same
-padded size, on every replay, with and without the graph."""
+"""GPU tests of the batched form (many catalogs, one persistent pair launch
+over every transform size or one per size, captured CUDA graph) and of the
+autotuner.  Each catalog of a batch must give exactly what the
+single-catalog FP32 path gives with the same plain size-P transform (the
+batched form never takes the overlap-save form), on every replay, with and
+without the graph."""
 import os
 
 import numpy as np
@@ -24,14 +26,17 @@ def _catalogs():
     return out
 
 
-@pytest.mark.parametrize("use_graph", [True, False])
-def test_batch_matches_single_catalog_path(cuda_ok, use_graph):
+@pytest.mark.parametrize("use_graph,per_size", [(True, False), (False, False), (True, True)])
+def test_batch_matches_single_catalog_path(cuda_ok, monkeypatch, use_graph, per_size):
     import torch
     from seismic_gb300.batch import Batch
+    monkeypatch.setenv("SEISMIC_BLOCK_FORM", "off")  # the single-catalog path's plain transform
     cats = _catalogs()
     tens = [torch.from_numpy(ev).cuda() for ev, _ in cats]
-    b = Batch(tens, [s for _, s in cats], thresholds=[0.05] * len(cats), n_classes_hist=9, use_graph=use_graph)
+    b = Batch(tens, [s for _, s in cats], thresholds=[0.05] * len(cats), n_classes_hist=9, use_graph=use_graph,
+              per_size=per_size)
     assert b.pairs == sum(ev.shape[0] * (ev.shape[0] + 1) // 2 for ev, _ in cats)
+    assert b.kernels_per_run == (1 + 5 if per_size else 2)  # sizes 512 .. 8192 present, or one mixed launch
     for rep in range(2):  # replay twice: same results (histograms accumulate)
         b.run()
         torch.cuda.synchronize()
