@@ -127,7 +127,17 @@ struct PairArgs {
   // make the waits run out on a healthy GPU, which is how the abort path and
   // its error status are tested.
   unsigned wait_limit;
+  // Nonzero (SEISMIC_DEVICE_WAIT_PROBE): the producer's first wait is on a
+  // barrier nothing ever completes, so it runs out after wait_limit polls
+  // -- the deterministic way for a test to take the abort path.
+  int wait_probe;
 };
+
+// SEISMIC_DEVICE_WAIT_PROBE set to a nonzero value.
+inline int device_wait_probe() {
+  const char *e = getenv("SEISMIC_DEVICE_WAIT_PROBE");
+  return (e && atoi(e) != 0) ? 1 : 0;
+}
 
 // Spectrum rows per event of the pair launch `a` (channels x blocks).
 __host__ __device__ inline int spectrum_rows(const PairArgs &a) {

@@ -156,6 +156,7 @@ struct LagArgs {
   int kgroup;     // K-chunks per MMA group (1 .. kLagGroupMax, at most stages / 2)
   long long blk_begin, blk_end;  // triangle: the 128-event blocks this launch walks
   unsigned wait_limit;  // polls of each bounded wait (0: kLagWaitPolls); SEISMIC_DEVICE_WAIT_POLLS
+  int wait_probe;       // the TMA warp's first wait is on a barrier nothing completes (SEISMIC_DEVICE_WAIT_PROBE)
 };
 
 struct LagSmem {  // offsets into dynamic shared memory (base 1024-aligned)
@@ -177,7 +178,7 @@ static LagSmem lag_smem_layout(const LagArgs &a) {
   s.bars = off;
   off += (2 * a.stages + 9) * 8;
   s.misc = off;
-  off += 16;
+  off += 24;  // TMEM address, abort flag, wait limit, the probe mbarrier (+16)
   s.total = off + 1024;  // room to align the base
   return s;
 }
@@ -338,6 +339,7 @@ __global__ void __launch_bounds__(kLagThreads, 1)
       tc::mbar_init(&tmem_empty[k], kLagM); // the 128 epilogue threads
     }
     tc::mbar_init(mma_drain, 1);
+    tc::mbar_init(reinterpret_cast<uint64_t *>(base + L.misc + 16), 1);  // the probe: never completed
     *abort_flag = 0;
     reinterpret_cast<volatile uint32_t *>(abort_flag)[1] = a.wait_limit ? a.wait_limit : kLagWaitPolls;
     tc::fence_mbarrier_init();
@@ -378,7 +380,9 @@ __global__ void __launch_bounds__(kLagThreads, 1)
       uint32_t phase = 0;
       long long it = 0;
       uint32_t issued_mask = 0, last_parity = 0;  // per stage: any load issued / parity of the latest
-      bool stop = false;  // uniform over the warp
+      // the test probe: a wait that nothing completes runs out before any load
+      bool stop = a.wait_probe &&
+                  !lag_wait_warp(reinterpret_cast<uint64_t *>(base + L.misc + 16), 0, abort_flag, a.error_flag);
       for (long long bb = b, qq = q; bb < nblk && !stop; advance_item(bb, qq, gridDim.x, N, a.jc, nblk, n_rect)) {
         const long long j_begin = (RECT ? 0 : bb * kLagM) + qq * a.jc;
         const long long j_end = min(j_begin + a.jc, n_j);
@@ -968,6 +972,7 @@ cudaError_t launch_lag_blocks(const void *ws, long long n, int C, int length, in
   a.min_hist = hmin;
   a.error_flag = error_flag;
   a.wait_limit = device_wait_polls();
+  a.wait_probe = device_wait_probe();
   a.blk_begin = blk_begin;
   a.blk_end = blk_end;
   long long items = 0;
@@ -1027,6 +1032,7 @@ cudaError_t launch_lag_rect(const void *cat_ws, long long n_cat, const void *q_w
   a.lags_neg = ln;
   a.error_flag = error_flag;
   a.wait_limit = device_wait_polls();
+  a.wait_probe = device_wait_probe();
   const long long nblk = (n_cols + kLagM - 1) / kLagM;
   const long long items = nblk * ((n_query + pl.jc - 1) / pl.jc);
   return launch_lag_kernel(a, pl, a.xhi, a.xlo, n_cat * C, items, sm_count, s);

@@ -68,7 +68,8 @@ template <int P, int NWARP, int RU> struct Staged {  // RU: chunks r per ring sl
   static constexpr size_t EX_BYTES = (size_t)NG * padded_len<P>() * sizeof(float2);
   static constexpr size_t RED_BYTES = (size_t)NG * NW * 8 * sizeof(unsigned);
   static constexpr size_t PROD_OFF = (EX_BYTES + RED_BYTES + 15) / 16 * 16;
-  // producer area: cursor (48 B), abort flag, item ring of kItemRing (i, j0)
+  // producer area: cursor (48 B), abort flag (+48), probe mbarrier (+56),
+  // item ring of kItemRing (i, j0)
   static constexpr size_t ITEMS_OFF = PROD_OFF + 64;
   static constexpr size_t RING_OFF = (ITEMS_OFF + kItemRing * 16 + 127) / 128 * 128;
   // one chunk r of every staged row, and a ring slot of RU chunks
@@ -176,6 +177,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
   unsigned *reds = reinterpret_cast<unsigned *>(smem + SH::EX_BYTES);
   StagedCursor *cur = reinterpret_cast<StagedCursor *>(smem + SH::PROD_OFF);
   volatile int *s_abort = reinterpret_cast<volatile int *>(smem + SH::PROD_OFF + 48);
+  uint64_t *probe = reinterpret_cast<uint64_t *>(smem + SH::PROD_OFF + 56);  // never completed
   StagedItem *items = reinterpret_cast<StagedItem *>(smem + SH::ITEMS_OFF);
   unsigned char *ring = smem + SH::RING_OFF;
   const int K = a.ring;
@@ -188,6 +190,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
 
   if (threadIdx.x == 0) {
     *s_abort = 0;
+    tc::mbar_init(probe, 1);
     for (int k = 0; k < K; ++k) {
       tc::mbar_init(&full[k], 1);
       tc::mbar_init(&empty[k], SH::CONSUMERS);
@@ -214,7 +217,9 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       uint32_t phase = 0;
       const uint32_t limit = a.wait_limit ? a.wait_limit : kStagedWaitPolls;
       long long issued = 0;
-      for (long long u = 0; u < units_total; ++u) {
+      // the test probe: a wait that nothing completes runs out before any issue
+      const bool probed = a.wait_probe && !producer_wait(probe, 0, limit, s_abort, a.error_flag);
+      for (long long u = 0; u < units_total && !probed; ++u) {
         if (u >= K && !producer_wait(&empty[slot], phase ^ 1u, limit, s_abort, a.error_flag)) break;
         staged_issue<P, NWARP, RU, ST>(a, &jmap, cur, items, ring + (size_t)slot * UNIT, &full[slot]);
         ++issued;
@@ -390,6 +395,7 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
   }
   a.band_tiles = l2_band_tiles(spectrum_rows(a), P, (int)sizeof(ST_T), SH::T);
   a.wait_limit = device_wait_polls();
+  a.wait_probe = device_wait_probe();
 
   // Tensor map of the j spectra: dims {P/2 bins, C channels, N events},
   // box {S bins, 1 channel, T events}.
