@@ -197,24 +197,6 @@ template <int P, int DIR> struct TwiddleRoots {
   }
 };
 
-// The twiddle roots of one later pass, looked up ahead of it (their table
-// addresses depend only on t): issued before the exchange that precedes the
-// pass, their L1 latency hides behind its barrier instead of stalling the
-// pass.  w[0] when every job of the thread shares m = t mod NS, else w[q]
-// for job q -- the layout pass_compute takes as `roots`.
-template <int P, int R, int NS, int DIR>
-__device__ __forceinline__ void prefetch_roots(int t, const float2 *__restrict__ tw, float2 (&w)[32 / R]) {
-  constexpr int G = P / 32;
-  constexpr int J = 32 / R;
-  constexpr int step = kMaxP / (NS * R);
-  if constexpr (J > 1 && G % NS == 0) {
-    w[0] = twiddle_lookup<DIR>(tw, (t % NS) * step);
-  } else {
-#pragma unroll
-    for (int q = 0; q < J; ++q) w[q] = twiddle_lookup<DIR>(tw, ((t + q * G) % NS) * step);
-  }
-}
-
 // ------------------------------------------------------------- group sync
 // A group is G consecutive threads of a CTA.  Groups of <= 32 threads live in
 // one warp and sync with __syncwarp on their own lanes; larger groups use a

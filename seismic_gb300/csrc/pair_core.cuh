@@ -215,11 +215,7 @@ __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, 
                                                   const float2 *__restrict__ tw, const TwiddleRoots<P, 1> &roots,
                                                   bool *stop = nullptr) {
   using PL = FftPlan<P>;
-  using TR = TwiddleRoots<P, 1>;
   constexpr int G = P / 32;
-  // roots of the passes TwiddleRoots does not hold, looked up one exchange ahead
-  float2 w2[32 / PL::R2];
-  if constexpr (!TR::H2) prefetch_roots<P, PL::R2, 16, 1>(t, tw, w2);
   dft<16, 1>(&v[0]);
   dft<16, 1>(&v[16]);
 #pragma unroll
@@ -235,25 +231,19 @@ __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, 
   }
   pass_read<P, PL::R2>(buf, v, t);
   group_sync<G>(g);
-  pass_compute<P, PL::R2, 16, 1>(v, t, tw, TR::H2 ? roots.template get<2>() : w2);
+  pass_compute<P, PL::R2, 16, 1>(v, t, tw, roots.template get<2>());
   if constexpr (PL::R3 != 0) {
-    constexpr int R3 = PL::R3 ? PL::R3 : 1;
-    float2 w3[32 / R3];
-    if constexpr (!TR::H3) prefetch_roots<P, R3, 16 * PL::R2, 1>(t, tw, w3);
     pass_write<P, PL::R2, 16>(buf, v, t);
     group_sync<G>(g);
     pass_read<P, PL::R3>(buf, v, t);
     group_sync<G>(g);
-    pass_compute<P, PL::R3, 16 * PL::R2, 1>(v, t, tw, TR::H3 ? roots.template get<3>() : w3);
+    pass_compute<P, PL::R3, 16 * PL::R2, 1>(v, t, tw, roots.template get<3>());
     if constexpr (PL::R4 != 0) {
-      constexpr int R4 = PL::R4 ? PL::R4 : 1;
-      float2 w4[32 / R4];
-      if constexpr (!TR::H4) prefetch_roots<P, R4, 16 * PL::R2 * PL::R3, 1>(t, tw, w4);
       pass_write<P, PL::R3, 16 * PL::R2>(buf, v, t);
       group_sync<G>(g);
       pass_read<P, PL::R4>(buf, v, t);
       group_sync<G>(g);
-      pass_compute<P, PL::R4, 16 * PL::R2 * PL::R3, 1>(v, t, tw, TR::H4 ? roots.template get<4>() : w4);
+      pass_compute<P, PL::R4, 16 * PL::R2 * PL::R3, 1>(v, t, tw, roots.template get<4>());
     }
   }
 }
