@@ -34,7 +34,8 @@ struct SpectraArgs {
   // samples o_b .. o_b + P - 1, o_b = b * block_len - block_shift; the A
   // frame keeps samples b * block_len .. + block_len - 1 (zero elsewhere),
   // the W frame all of them.  A spectra go to `spectra`, W spectra to
-  // `spectra_w`, both [n_events*n_channels][blocks][P/2].
+  // `spectra_w`, both [n_events*n_channels][blocks][P/2]; a null pointer
+  // leaves that set out (a serving catalog keeps only W, queries only A).
   int blocks;
   int block_len;
   int block_shift;

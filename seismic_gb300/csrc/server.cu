@@ -153,6 +153,11 @@ struct seismic_server {
   // catalog
   long long n_cat = 0;
   int C = 0, L = 0, P = 0, shift = 0, stype = 0, prescale = 0, topk = 16;
+  // FFT forms: the overlap-save plan of the lag window (nb == 0: plain size-P
+  // transforms).  With a plan the catalog keeps its W frames and each request
+  // transforms its queries into A frames; PT is the pair kernel's size.
+  BlockPlan bp;
+  int PT = 0;
   float threshold = 0.f;
   void *cat_spectra = nullptr;
   double *cat_norms = nullptr;
@@ -200,10 +205,40 @@ size_t round256(size_t v) { return (v + 255) & ~(size_t)255; }
 
 // Bytes of the per-request transforms of the queries: spectra + norms, or the
 // lag form's planes + norms.
+// Bytes of one (plain or A-frame) spectra array of `rows` event rows.
+size_t spectra_rows_bytes(const seismic_server *s, size_t rows) {
+  return round256(rows * (size_t)(s->bp.nb ? s->bp.nb : 1) * (s->PT / 2) * (s->stype ? 4 : 8));
+}
+
 size_t query_prep_bytes(const seismic_server *s, int nq) {
   const size_t rows = (size_t)nq * s->C;
   if (s->lag_form) return round256(lag_workspace_bytes(nq, s->C, s->L, lag_planes(s->lag_form)));
-  return round256(rows * (s->P / 2) * (s->stype ? 4 : 8)) + norms_buffer_bytes((long long)rows);
+  return spectra_rows_bytes(s, rows) + norms_buffer_bytes((long long)rows);
+}
+
+// Kernel (a) of `n` events into `spectra` (plain) or, with a plan, into the A
+// frames (`spectra`) and / or the W frames (`spectra_w`).
+cudaError_t server_spectra(const seismic_server *s, const float *events, long long n, void *spectra,
+                           void *spectra_w, double *norms, cudaStream_t st) {
+  SpectraArgs sa{};
+  sa.events = events;
+  sa.n_events = n;
+  sa.n_channels = s->C;
+  sa.length = s->L;
+  sa.ev_stride = (long long)s->C * s->L;
+  sa.ch_stride = s->L;
+  sa.prescale = s->prescale;
+  sa.stype = s->stype;
+  sa.spectra = spectra;
+  sa.spectra_w = spectra_w;
+  sa.norms = norms;
+  sa.inv_norms = inverse_norms_of(norms, n * s->C);
+  sa.twiddles = s->tw;
+  if (!s->bp.nb) return launch_spectra(s->P, sa, st);
+  sa.blocks = s->bp.nb;
+  sa.block_len = s->bp.B;
+  sa.block_shift = s->shift;
+  return launch_block_spectra(s->PT, sa, st);
 }
 
 size_t request_bytes(const seismic_server *s, int nq, long long ncols) {
@@ -276,7 +311,7 @@ int launch_request(seismic_server *s, Request *r) {
   float *q_ev = reinterpret_cast<float *>(base);
   base += round256(rows * s->L * sizeof(float));
   void *q_spec = base;  // spectra, or the lag form's planes
-  double *q_norm = reinterpret_cast<double *>(base + round256(rows * (s->P / 2) * (s->stype ? 4 : 8)));
+  double *q_norm = reinterpret_cast<double *>(base + (s->lag_form ? 0 : spectra_rows_bytes(s, rows)));
   base += query_prep_bytes(s, nq);
   const size_t ob = round256((size_t)nq * r->n_cols * 4);
   float *d_vp = reinterpret_cast<float *>(base);
@@ -307,20 +342,8 @@ int launch_request(seismic_server *s, Request *r) {
                           s->threshold, s->lag_form, d_vp, d_lp, d_vn, d_ln, s->error_flag, pair_sms(s), st);
     note_launches(2);
   } else {
-  SpectraArgs sa{};
-  sa.events = q_ev;
-  sa.n_events = nq;
-  sa.n_channels = s->C;
-  sa.length = s->L;
-  sa.ev_stride = (long long)s->C * s->L;
-  sa.ch_stride = s->L;
-  sa.prescale = s->prescale;
-  sa.stype = s->stype;
-  sa.spectra = q_spec;
-  sa.norms = q_norm;
-  sa.inv_norms = inverse_norms_of(q_norm, (long long)rows);
-  sa.twiddles = s->tw;
-  if (e == cudaSuccess) e = launch_spectra(s->P, sa, st);
+  // the queries' spectra (the A frames with an overlap-save plan)
+  if (e == cudaSuccess) e = server_spectra(s, q_ev, nq, q_spec, nullptr, q_norm, st);
   PairArgs pa{};
   pa.rect = 1;
   pa.spectra = s->cat_spectra;
@@ -346,9 +369,10 @@ int launch_request(seismic_server *s, Request *r) {
   pa.twiddles = s->tw;
   pa.error_flag = s->error_flag;
   pa.couple_begin = 0;
-  pa.couple_end = pair_work_total(s->P, pa);
+  pa.spec_channels = s->bp.nb ? s->C * s->bp.nb : 0;  // catalog W frames (j), query A frames (i)
+  pa.couple_end = pair_work_total(s->PT, pa);
   if (e == cudaSuccess && s->last_pair) e = cudaStreamWaitEvent(st, s->last_pair, 0);
-  if (e == cudaSuccess) e = launch_pair_work(s->P, pa, pair_sms(s), 0, st);
+  if (e == cudaSuccess) e = launch_pair_work(s->PT, pa, pair_sms(s), 0, st);
   }
   if (e == cudaSuccess) e = cudaEventRecord(s->pair_done[r->slot], st);
   if (e == cudaSuccess) s->last_pair = s->pair_done[r->slot];
@@ -453,6 +477,8 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   s->stype = form == SEISMIC_FORM_FP16_SPECTRA ? 1 : 0;
   s->lag_form = lag ? form : 0;
   s->prescale = (n_channels > 1 || s->stype) ? 1 : 0;
+  if (!lag) s->bp = block_plan(event_length, shift, P, n_channels, s->stype);
+  s->PT = s->bp.nb ? s->bp.Q : P;
   s->topk = topk;
   s->sm_count = sm;
   s->tw = tw;
@@ -472,7 +498,7 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
   if (lag) {
     e = cudaMalloc(&s->cat_lag, lag_workspace_bytes(n_catalog, n_channels, event_length, lag_planes(form)));
   } else {
-    e = cudaMalloc(&s->cat_spectra, (size_t)rows * (P / 2) * (s->stype ? 4 : 8));
+    e = cudaMalloc(&s->cat_spectra, spectra_rows_bytes(s, (size_t)rows));
     if (e == cudaSuccess) e = cudaMalloc(&s->cat_norms, norms_buffer_bytes(rows));
   }
   if (e == cudaSuccess) e = cudaMalloc(&d_cat, (size_t)rows * event_length * sizeof(float));
@@ -484,20 +510,9 @@ extern "C" int seismic_server_create(const float *catalog, long long n_catalog, 
     note_launches(1);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
   } else if (e == cudaSuccess) {
-    SpectraArgs sa{};
-    sa.events = d_cat;
-    sa.n_events = n_catalog;
-    sa.n_channels = n_channels;
-    sa.length = event_length;
-    sa.ev_stride = (long long)n_channels * event_length;
-    sa.ch_stride = event_length;
-    sa.prescale = s->prescale;
-    sa.stype = s->stype;
-    sa.spectra = s->cat_spectra;
-    sa.norms = s->cat_norms;
-    sa.inv_norms = inverse_norms_of(s->cat_norms, rows);
-    sa.twiddles = tw;
-    e = launch_spectra(P, sa, nullptr);
+    // the catalog's spectra (the W frames with an overlap-save plan)
+    e = s->bp.nb ? server_spectra(s, d_cat, n_catalog, nullptr, s->cat_spectra, s->cat_norms, nullptr)
+                 : server_spectra(s, d_cat, n_catalog, s->cat_spectra, nullptr, s->cat_norms, nullptr);
     note_launches(1);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
   }

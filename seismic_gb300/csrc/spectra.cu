@@ -408,8 +408,8 @@ __global__ void __launch_bounds__(256) block_spectra_kernel(SpectraArgs a) {
         va = make_float2(A.x * scale, A.y * scale);
         vw = make_float2(W.x * scale, W.y * scale);
       }
-      store_spectrum(a.spectra, a.stype, off + k, va);
-      store_spectrum(a.spectra_w, a.stype, off + k, vw);
+      if (a.spectra) store_spectrum(a.spectra, a.stype, off + k, va);  // either may be left out
+      if (a.spectra_w) store_spectrum(a.spectra_w, a.stype, off + k, vw);
     }
   }
 }
