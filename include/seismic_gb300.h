@@ -300,6 +300,12 @@ int seismic_batch_kernels_per_run(const seismic_batch *batch);
 int seismic_autotune(int padded_size, int n_channels, const char *cache_path);
 /* The parameters currently used for (P, n_channels). */
 int seismic_tuning(int padded_size, int n_channels, int *tile, int *ctas_per_sm, int *item_groups);
+/* The TMA-staged form's CTA shape the autotuner cached for exactly
+ * (padded_size, n_channels spectrum rows per event): FFT warps per CTA (12,
+ * or 99 for the widest CTA that keeps 128 registers a thread) and spectral
+ * chunks per ring slot; both 0 when nothing is cached (the built-in rule
+ * applies).  No counterpart in the reference. */
+int seismic_tuning_staged(int padded_size, int n_channels, int *staged_warps, int *chunks_per_slot);
 
 /* ---- serving loop --------------------------------------------------------
  * A catalog kept resident on the device as packed half spectra (FP32 or

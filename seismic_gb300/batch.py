@@ -42,6 +42,9 @@ def _declare(lib):
     lib.seismic_tuning.restype = ctypes.c_int
     lib.seismic_tuning.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                    ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    lib.seismic_tuning_staged.restype = ctypes.c_int
+    lib.seismic_tuning_staged.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_int)]
     lib._batch_declared = True
     return lib
 
@@ -119,4 +122,7 @@ def tuning(padded_size: int, n_channels: int) -> dict:
     lib = _declare(_lib.lib())
     t, c, i = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
     _lib.check(lib.seismic_tuning(padded_size, n_channels, ctypes.byref(t), ctypes.byref(c), ctypes.byref(i)))
-    return {"tile": t.value, "ctas_per_sm": c.value, "item_groups": i.value}
+    w, r = ctypes.c_int(), ctypes.c_int()
+    _lib.check(lib.seismic_tuning_staged(padded_size, n_channels, ctypes.byref(w), ctypes.byref(r)))
+    return {"tile": t.value, "ctas_per_sm": c.value, "item_groups": i.value, "staged_warps": w.value,
+            "staged_ru": r.value}

@@ -64,7 +64,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), srcs))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", tmp, *objs]
+    # -z defs: an unresolved symbol fails the build instead of the first dlopen
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "shared", "-Xlinker", "-z", "-Xlinker", "defs", "-o", tmp, *objs]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr}")

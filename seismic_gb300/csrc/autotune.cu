@@ -1,14 +1,21 @@
 // Autotuner for the pair kernel.
 //
-// For a padded size P and channel count C it times, on the current device,
-// the pair kernel over candidate tile sizes (events per tile side: how many
-// couples share one event's spectrum in L1) and CTAs per SM, then the
-// batched kernel over work-item sizes (couples per item, in units of the
-// CTA's groups), on a synthetic catalog sized so one launch takes ~10-50 ms.
+// For a transform size P and C spectrum rows per event (channels, times the
+// frames of the overlap-save form) it times, on the current device, on a
+// synthetic catalog sized so one launch takes ~10-50 ms:
+//  * the direct-load form over tile sizes (events per tile side: how many
+//    couples share one event's spectrum in L1) and CTAs per SM;
+//  * the TMA-staged form (P = 512 .. 4096) over its CTA shapes: FFT warps
+//    per CTA (12, or the widest that keeps 128 registers a thread), which
+//    sets the pairs per work item, and spectral chunks per ring slot;
+//  * the batched kernel over work-item sizes (couples per item, in units of
+//    the CTA's groups).
 // The fastest parameters go into an in-process table (used by every later
 // launch in this process) and into a text cache file, one line per (P, C):
-//   P=<P> C=<C> tile=<t> ctas=<k> item=<g> us=<time> gpu=<name>
-// Lookups fall back to (P, any C), then to built-in defaults.
+//   P=<P> C=<C> tile=<t> ctas=<k> item=<g> us=<time> gpu=<name> warps=<w> ru=<r>
+// Lookups of the direct-form and batched parameters fall back to (P, any C),
+// then to built-in defaults; the staged shape is used for the exact (P, C)
+// only.
 #include <sys/stat.h>
 
 #include <algorithm>
@@ -55,6 +62,10 @@ void load_file(const std::string &path) {
     if (sscanf(line, "P=%d C=%d tile=%d ctas=%d item=%d us=%lf gpu=%255s", &e.P, &e.C, &e.t.tile,
                &e.t.ctas_per_sm, &e.t.item_groups, &e.us, gpu) >= 5) {
       if (e.t.tile < 2 || e.t.tile > 64 || (e.t.tile & 1) || e.t.item_groups < 1) continue;
+      const char *w = strstr(line, " warps=");
+      const char *r = strstr(line, " ru=");
+      e.t.staged_warps = w ? atoi(w + 7) : 0;
+      e.t.staged_ru = r ? atoi(r + 4) : 0;
       e.gpu = gpu;
       bool replaced = false;
       for (auto &x : g_table)
@@ -85,8 +96,9 @@ bool write_file(const std::string &path) {
   FILE *f = fopen(path.c_str(), "w");
   if (!f) return false;
   for (const auto &e : g_table)
-    fprintf(f, "P=%d C=%d tile=%d ctas=%d item=%d us=%.1f gpu=%s\n", e.P, e.C, e.t.tile, e.t.ctas_per_sm,
-            e.t.item_groups, e.us, e.gpu.empty() ? "unknown" : e.gpu.c_str());
+    fprintf(f, "P=%d C=%d tile=%d ctas=%d item=%d us=%.1f gpu=%s warps=%d ru=%d\n", e.P, e.C, e.t.tile,
+            e.t.ctas_per_sm, e.t.item_groups, e.us, e.gpu.empty() ? "unknown" : e.gpu.c_str(), e.t.staged_warps,
+            e.t.staged_ru);
   fclose(f);
   return true;
 }
@@ -103,11 +115,24 @@ TuneEntry tune_lookup(int P, int n_channels) {
     if (!any) any = &e;
   }
   if (any) return any->t;
-  TuneEntry d;
+  TuneEntry d{};
   d.tile = pair_tile_for(P);
   d.ctas_per_sm = 0;
   d.item_groups = 16;
   return d;
+}
+
+bool tune_staged_lookup(int P, int spec_rows, int *warps, int *ru) {
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  ensure_loaded();
+  for (const auto &e : g_table) {
+    if (e.P == P && e.C == spec_rows && e.t.staged_warps > 0) {
+      *warps = e.t.staged_warps;
+      *ru = e.t.staged_ru;
+      return true;
+    }
+  }
+  return false;
 }
 
 }  // namespace seismic
@@ -132,6 +157,17 @@ extern "C" int seismic_tuning(int padded_size, int n_channels, int *tile, int *c
   if (tile) *tile = t.tile;
   if (ctas_per_sm) *ctas_per_sm = t.ctas_per_sm;
   if (item_groups) *item_groups = t.item_groups;
+  return SEISMIC_OK;
+}
+
+extern "C" int seismic_tuning_staged(int padded_size, int n_channels, int *staged_warps, int *chunks_per_slot) {
+  report_status(SEISMIC_OK, "");
+  if (!supported_padded_size(padded_size) || n_channels < 1)
+    return report_status(SEISMIC_ERR_UNSUPPORTED_SIZE, "unsupported padded size or channel count");
+  int w = 0, ru = 0;
+  if (!tune_staged_lookup(padded_size, n_channels, &w, &ru)) w = ru = 0;
+  if (staged_warps) *staged_warps = w;
+  if (chunks_per_slot) *chunks_per_slot = ru;
   return SEISMIC_OK;
 }
 
@@ -242,7 +278,7 @@ extern "C" int seismic_autotune(int padded_size, int n_channels, const char *cac
   };
 
   const int max_ctas = std::max(1, pair_ctas_per_sm(P));
-  TuneEntry bestT{pair_tile_for(P), 0, 16};
+  TuneEntry bestT{pair_tile_for(P), 0, 16, 0, 0};
   double best_us = 1e30;
   const int tiles[] = {2, 4, 8, 16};
   for (int tile : tiles) {
@@ -252,6 +288,37 @@ extern "C" int seismic_autotune(int padded_size, int n_channels, const char *cac
         best_us = us;
         bestT.tile = tile;
         bestT.ctas_per_sm = ctas;
+      }
+    }
+  }
+
+  // the staged form's CTA shape (FFT warps per CTA x chunks per ring slot)
+  if (P >= 512 && P <= 4096 && staged_enabled()) {
+    const int shapes[3][2] = {{12, 4}, {12, 2}, {99, 2}};  // 99: the widest CTA of this P
+    double best_staged = 1e30;
+    for (const auto &sh : shapes) {
+      PairArgs sa2 = pa;
+      sa2.staged_warps = sh[0];
+      sa2.staged_ru = sh[1];
+      sa2.tile = bestT.tile;
+      sa2.error_flag = err_flag;
+      sa2.couple_begin = 0;
+      sa2.couple_end = pair_work_total(P, sa2);
+      double best = 1e30;
+      for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(e0, st);
+        if (launch_pair_work(P, sa2, sm_count, 0, st) != cudaSuccess) break;
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best = std::min(best, (double)ms * 1e3);
+      }
+      note_launches(3);
+      if (best < best_staged) {
+        best_staged = best;
+        bestT.staged_warps = sh[0] == 12 ? 12 : 99;
+        bestT.staged_ru = sh[1];
       }
     }
   }

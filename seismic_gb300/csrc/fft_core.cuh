@@ -170,32 +170,95 @@ __device__ __forceinline__ void apply_twiddles(float2 *v, int m, const float2 *_
   }
 }
 
-// Twiddle roots w1 = exp(DIR 2 pi i m / (NS R)) of every job of the radix-16
-// passes after the first.  They depend only on the thread index, so a
-// persistent kernel loads them once; passes of smaller radix look theirs up.
+// cos and sin of x for |x| <= pi, in double at compile time (Taylor series
+// to the 41st power: far below double rounding there).
+constexpr double ct_sin(double x) {
+  double term = x, sum = x;
+  for (int n = 1; n <= 20; ++n) {
+    term *= -x * x / ((2.0 * n) * (2.0 * n + 1.0));
+    sum += term;
+  }
+  return sum;
+}
+constexpr double ct_cos(double x) {
+  double term = 1.0, sum = 1.0;
+  for (int n = 1; n <= 20; ++n) {
+    term *= -x * x / ((2.0 * n - 1.0) * (2.0 * n));
+    sum += term;
+  }
+  return sum;
+}
+
+// v * exp(DIR 2 pi i NUM / DEN), the root rounded once from double at compile
+// time: exp(i a) = -exp(i (a - pi)) with a - pi in [-pi, pi).
+template <int NUM, int DEN, int DIR> __device__ __forceinline__ float2 mul_turn(float2 v) {
+  constexpr int k = ((NUM % DEN) + DEN) % DEN;
+  if constexpr (k == 0) {
+    return v;
+  } else {
+    constexpr double x = 6.28318530717958647692528676655900577 * k / DEN - 3.14159265358979323846264338327950288;
+    constexpr float c = (float)(-ct_cos(x));
+    constexpr float s = (float)(-ct_sin(x) * DIR);
+    return cmul(v, make_float2(c, s));
+  }
+}
+
+// Twiddle roots of the passes after the first, held by a persistent kernel
+// (they depend only on the thread index).  In every plan each later pass is
+// one of two kinds, both served by ONE root r_t = exp(DIR 2 pi i t / (NS R)):
+//  * uniform (G % NS == 0): every job of the thread has m = t mod NS = t;
+//  * base (the thread's J jobs have m = t + q G < NS): job q's root is r_t
+//    times the compile-time root exp(DIR 2 pi i q G / (NS R)) (mul_turn).
+// So no pass looks a twiddle up in the pair loop.
 template <int P, int DIR> struct TwiddleRoots {
   using PL = FftPlan<P>;
   static constexpr int G = P / 32;
   static constexpr int NS2 = 16, NS3 = 16 * PL::R2, NS4 = 16 * PL::R2 * (PL::R3 ? PL::R3 : 1);
-  static constexpr bool H2 = PL::R2 == 16, H3 = PL::R3 == 16, H4 = PL::R4 == 16;
-  float2 w2[H2 ? 2 : 1], w3[H3 ? 2 : 1], w4[H4 ? 2 : 1];
+  float2 w2, w3, w4;
 
   __device__ __forceinline__ void load(int t, const float2 *__restrict__ tw) {
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int j = t + q * G;
-      if constexpr (H2) w2[q] = twiddle_lookup<DIR>(tw, (j % NS2) * (kMaxP / (NS2 * 16)));
-      if constexpr (H3) w3[q] = twiddle_lookup<DIR>(tw, (j % NS3) * (kMaxP / (NS3 * 16)));
-      if constexpr (H4) w4[q] = twiddle_lookup<DIR>(tw, (j % NS4) * (kMaxP / (NS4 * 16)));
-    }
+    w2 = twiddle_lookup<DIR>(tw, (t % NS2) * (kMaxP / (NS2 * PL::R2)));
+    if constexpr (PL::R3 != 0) w3 = twiddle_lookup<DIR>(tw, (t % NS3) * (kMaxP / (NS3 * PL::R3)));
+    if constexpr (PL::R4 != 0) w4 = twiddle_lookup<DIR>(tw, (t % NS4) * (kMaxP / (NS4 * PL::R4)));
   }
-  // roots of pass `pass` (2, 3 or 4), or nullptr when that pass looks them up
-  template <int PASS> __device__ __forceinline__ const float2 *get() const {
-    if constexpr (PASS == 2) return H2 ? w2 : nullptr;
-    else if constexpr (PASS == 3) return H3 ? w3 : nullptr;
-    else return H4 ? w4 : nullptr;
+  template <int PASS> __device__ __forceinline__ float2 get() const {
+    if constexpr (PASS == 2) return w2;
+    else if constexpr (PASS == 3) return w3;
+    else return w4;
   }
 };
+
+// Job q of a pass served by a held root (TwiddleRoots): twiddles then DFT_R,
+// for q = Q .. J-1.
+template <int P, int R, int NS, int DIR, int Q = 0>
+__device__ __forceinline__ void base_root_jobs(float2 (&v)[32], float2 root) {
+  constexpr int G = P / 32;
+  constexpr int J = 32 / R;
+  if constexpr (Q < J) {
+    apply_root_powers<R>(&v[Q * R], mul_turn<Q * G, NS * R, DIR>(root));
+    dft<R, DIR>(&v[Q * R]);
+    base_root_jobs<P, R, NS, DIR, Q + 1>(v, root);
+  }
+}
+
+// A later pass with its held root (uniform or base kind, see TwiddleRoots).
+template <int P, int R, int NS, int DIR>
+__device__ __forceinline__ void pass_compute_held(float2 (&v)[32], float2 root) {
+  constexpr int G = P / 32;
+  constexpr int J = 32 / R;
+  static_assert(NS > 1 && (G % NS == 0 || J * G <= NS), "pass_compute_held: root not of one kind");
+  if constexpr (G % NS == 0) {
+    float2 w[R];
+    root_powers<R>(root, w);
+#pragma unroll
+    for (int q = 0; q < J; ++q) {
+      apply_powers<R>(&v[q * R], w);
+      dft<R, DIR>(&v[q * R]);
+    }
+  } else {
+    base_root_jobs<P, R, NS, DIR>(v, root);
+  }
+}
 
 // ------------------------------------------------------------- group sync
 // A group is G consecutive threads of a CTA.  Groups of <= 32 threads live in

@@ -123,6 +123,10 @@ struct PairArgs {
   // rows per event (n_channels * blocks; 0 = n_channels).
   const void *spectra_i;
   int spec_channels;
+  // Staged form: a CTA shape forced by the autotuner while it times the
+  // candidates (FFT warps per CTA, chunks per ring slot; 0 = not forced).
+  int staged_warps;
+  int staged_ru;
   // Poll limit of the staged form's producer waits (0: the built-in limit,
   // seconds of back-off).  Set from SEISMIC_DEVICE_WAIT_POLLS: a few polls
   // make the waits run out on a healthy GPU, which is how the abort path and
@@ -246,8 +250,12 @@ struct TuneEntry {
   int tile;          // events per tile side
   int ctas_per_sm;   // 0 = occupancy maximum
   int item_groups;   // couples per batched work item, in units of groups per CTA
+  int staged_warps;  // staged form: FFT warps per CTA (0: the built-in rule)
+  int staged_ru;     // staged form, FP32 spectra: chunks per ring slot (0: the built-in rule)
 };
 TuneEntry tune_lookup(int P, int n_channels);
+// The staged form's tuned CTA shape for exactly (P, spectrum rows), if any.
+bool tune_staged_lookup(int P, int spec_rows, int *warps, int *ru);
 
 // ---- lag-GEMM form (laggemm.cu): time-domain lag sums on tcgen05 tensor cores
 struct LagPlan {

@@ -231,19 +231,19 @@ __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, 
   }
   pass_read<P, PL::R2>(buf, v, t);
   group_sync<G>(g);
-  pass_compute<P, PL::R2, 16, 1>(v, t, tw, roots.template get<2>());
+  pass_compute_held<P, PL::R2, 16, 1>(v, roots.template get<2>());
   if constexpr (PL::R3 != 0) {
     pass_write<P, PL::R2, 16>(buf, v, t);
     group_sync<G>(g);
     pass_read<P, PL::R3>(buf, v, t);
     group_sync<G>(g);
-    pass_compute<P, PL::R3, 16 * PL::R2, 1>(v, t, tw, roots.template get<3>());
+    pass_compute_held<P, PL::R3, 16 * PL::R2, 1>(v, roots.template get<3>());
     if constexpr (PL::R4 != 0) {
       pass_write<P, PL::R3, 16 * PL::R2>(buf, v, t);
       group_sync<G>(g);
       pass_read<P, PL::R4>(buf, v, t);
       group_sync<G>(g);
-      pass_compute<P, PL::R4, 16 * PL::R2 * PL::R3, 1>(v, t, tw, roots.template get<4>());
+      pass_compute_held<P, PL::R4, 16 * PL::R2 * PL::R3, 1>(v, roots.template get<4>());
     }
   }
 }

@@ -332,23 +332,41 @@ constexpr int kStagedWarps = 12;  // FFT warps per CTA, plus the producer warp
 // in whole groups of P/32 threads.
 constexpr int staged_wide_warps(int P) { return P >= 4096 ? 12 : (P == 2048 ? 14 : 15); }
 
-// FFT warps the dispatch uses.  The wide CTA (more FFT warps, a smaller
-// ring) wins where one channel's item fits it: one channel at P = 2048 (FP32
-// spectra 263 vs 230 M pairs/s measured, FP16 256 vs 233, BF16 255 vs 237;
-// with three channels 175 vs 184).  SEISMIC_STAGED_WARPS=wide / =12 forces
-// either.
-static int staged_nwarp(int P, int stype, int n_channels) {
-  const char *e = getenv("SEISMIC_STAGED_WARPS");
-  if (e && strcmp(e, "wide") == 0) return staged_wide_warps(P);
-  if (e && strcmp(e, "12") == 0) return kStagedWarps;
-  return (P == 2048 && n_channels == 1) ? staged_wide_warps(P) : kStagedWarps;
-}
-
-// Chunks per ring slot: 4 (half the slot waits and releases of 2, a ring of
-// two to four slots), or 2 for FP32 spectra when SEISMIC_STAGED_RU=2.
-static int staged_ru() {
-  const char *e = getenv("SEISMIC_STAGED_RU");
-  return (e && strcmp(e, "2") == 0) ? 2 : 4;
+// CTA shape of a launch: FFT warps per CTA and chunks per ring slot.  In
+// order: a shape the autotuner forces while timing, SEISMIC_STAGED_WARPS /
+// SEISMIC_STAGED_RU, the tuner's cached choice for exactly (P, spectrum
+// rows), else the built-in rule: the wide CTA (more FFT warps, a smaller
+// ring) where one spectrum row's item fits it -- one channel at P = 2048
+// (FP32 spectra 263 vs 230 M pairs/s measured, FP16 256 vs 233, BF16 255 vs
+// 237; with three channels 175 vs 184) -- and 4-chunk slots otherwise.  The
+// wide FP32 CTA has room for 2-chunk slots only; half-precision spectra
+// always take 4.
+struct StagedShape {
+  int nwarp, ru;
+};
+static StagedShape staged_shape(int P, const PairArgs &a) {
+  const int rows = spectrum_rows(a);
+  int w = a.staged_warps, ru = a.staged_ru;
+  if (!w) {
+    const char *e = getenv("SEISMIC_STAGED_WARPS");
+    if (e && strcmp(e, "wide") == 0) w = staged_wide_warps(P);
+    if (e && strcmp(e, "12") == 0) w = kStagedWarps;
+  }
+  if (!ru) {
+    const char *e = getenv("SEISMIC_STAGED_RU");
+    if (e && strcmp(e, "2") == 0) ru = 2;
+  }
+  int tw = 0, tru = 0;
+  if ((!w || !ru) && tune_staged_lookup(P, rows, &tw, &tru)) {
+    if (!w) w = tw;
+    if (!ru) ru = tru;
+  }
+  if (!w) w = (P == 2048 && rows == 1) ? staged_wide_warps(P) : kStagedWarps;
+  w = (w == kStagedWarps) ? kStagedWarps : staged_wide_warps(P);
+  if (a.stype != 0) ru = 4;                       // half spectra: 4-chunk slots
+  else if (w != kStagedWarps) ru = 2;             // the wide FP32 CTA: 2-chunk slots
+  else ru = (ru == 2) ? 2 : 4;
+  return StagedShape{w, ru};
 }
 
 // The staged form serves P = 512 .. 4096: there the three rows of a couple
@@ -367,7 +385,7 @@ bool staged_supported(int P, const PairArgs &a) {
   return tensor_map_encoder() != nullptr;
 }
 
-int staged_tile_side(int P, const PairArgs &a) { return 2 * (staged_nwarp(P, a.stype, spectrum_rows(a)) * 32 / (P / 32)); }
+int staged_tile_side(int P, const PairArgs &a) { return 2 * (staged_shape(P, a).nwarp * 32 / (P / 32)); }
 
 long long staged_items_total(int P, const PairArgs &a) {
   const long long T = staged_tile_side(P, a);
@@ -418,19 +436,19 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
 }
 
 template <int P> static cudaError_t launch_staged_p(const PairArgs &a, int sm_count, cudaStream_t s) {
+  const StagedShape sh = staged_shape(P, a);
+  const bool wide = sh.nwarp != kStagedWarps;
   switch (a.stype) {
     case 0:
-      // the wide CTA's exchange buffers leave room for a ring of 2-chunk slots
-      if (staged_nwarp(P, 0, spectrum_rows(a)) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 2, 0>(a, sm_count, s);
-      return staged_ru() == 2 ? launch_staged_t<P, kStagedWarps, 2, 0>(a, sm_count, s)
-                              : launch_staged_t<P, kStagedWarps, 4, 0>(a, sm_count, s);
-    // half-precision spectra: half the ring bytes, so the wide CTA keeps 4-chunk slots
+      if (wide) return launch_staged_t<P, staged_wide_warps(P), 2, 0>(a, sm_count, s);
+      return sh.ru == 2 ? launch_staged_t<P, kStagedWarps, 2, 0>(a, sm_count, s)
+                        : launch_staged_t<P, kStagedWarps, 4, 0>(a, sm_count, s);
     case 1:
-      if (staged_nwarp(P, 1, spectrum_rows(a)) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 4, 1>(a, sm_count, s);
-      return launch_staged_t<P, kStagedWarps, 4, 1>(a, sm_count, s);
+      return wide ? launch_staged_t<P, staged_wide_warps(P), 4, 1>(a, sm_count, s)
+                  : launch_staged_t<P, kStagedWarps, 4, 1>(a, sm_count, s);
     case 2:
-      if (staged_nwarp(P, 2, spectrum_rows(a)) != kStagedWarps) return launch_staged_t<P, staged_wide_warps(P), 4, 2>(a, sm_count, s);
-      return launch_staged_t<P, kStagedWarps, 4, 2>(a, sm_count, s);
+      return wide ? launch_staged_t<P, staged_wide_warps(P), 4, 2>(a, sm_count, s)
+                  : launch_staged_t<P, kStagedWarps, 4, 2>(a, sm_count, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -56,8 +56,9 @@ def test_autotuner_writes_cache_and_is_used(cuda_ok, tmp_path):
     path = os.path.join(tmp_path, "tune.txt")
     t = batch.autotune(1024, 1, path)
     assert t["tile"] in (2, 4, 8, 16) and t["ctas_per_sm"] >= 1 and t["item_groups"] in (4, 16, 64)
+    assert t["staged_warps"] in (12, 99) and t["staged_ru"] in (2, 4)   # the staged form's CTA shape
     line = open(path).read()
-    assert f"P=1024 C=1 tile={t['tile']}" in line
+    assert f"P=1024 C=1 tile={t['tile']}" in line and f"warps={t['staged_warps']} ru={t['staged_ru']}" in line
     assert batch.tuning(1024, 1) == t
     # results do not depend on the tuned parameters
     ev = synth.ricker_catalog(70, 512, seed=9)
