@@ -286,6 +286,15 @@ __device__ __forceinline__ void scan_and_write(const PairArgs &a, float2 (&v)[32
   constexpr int RL = PL::R4 ? PL::R4 : (PL::R3 ? PL::R3 : PL::R2);
   const int d0 = 1 - a.shift;
   const unsigned gmask = group_lane_mask<G>();
+  // the couple's inverse norms (one-channel forms), loaded before the scan
+  // so their latency overlaps it; thread 0 of the group uses them below
+  float2 pre_ni = make_float2(0.f, 0.f), pre_nja = pre_ni, pre_njb = pre_ni;
+  if (t == 0 && !a.prescaled) {
+    const int C = a.n_channels;
+    pre_ni = (a.rect ? a.inv_norms_q : a.inv_norms)[ia * C];
+    pre_nja = a.inv_norms[ja * C];
+    pre_njb = a.inv_norms[jb * C];
+  }
 
   // ---- phase A: per-thread max / min of both series.  Values outside the
   //      lag window (wmask = window_mask<P>(t, a.shift)) are zeroed: 0 never
@@ -385,7 +394,7 @@ __device__ __forceinline__ void scan_and_write(const PairArgs &a, float2 (&v)[32
         for (int c = 0; c < C; ++c) live |= (inv_i[i * C + c].x > 0.f) && (a.inv_norms[j * C + c].x > 0.f);
         scale = reciprocal_pair(C);
       } else {
-        const float2 ni = inv_i[i * C], nj = a.inv_norms[j * C];
+        const float2 ni = pre_ni, nj = p == 0 ? pre_nja : pre_njb;  // ia == ib: one event i per couple
         live = ni.x > 0.f && nj.x > 0.f;
         scale = product_pair(ni, nj);
       }
