@@ -78,6 +78,14 @@ static std::vector<DeviceState> g_devices;
 // Pair launches per host call: the device-to-host copy of each chunk's
 // outputs overlaps the next chunk's kernel.
 constexpr int kHostChunks = 8;
+// SEISMIC_HOST_CHUNKS (1 .. 64) overrides the chunk count.
+static int host_chunks() {
+  if (const char *e = getenv("SEISMIC_HOST_CHUNKS")) {
+    const int v = atoi(e);
+    if (v >= 1 && v <= 64) return v;
+  }
+  return kHostChunks;
+}
 
 // Packed index of pair (i, i): where row i of the upper triangle starts.
 static long long packed_row_start(long long i, long long n) { return i * n - i * (i - 1) / 2; }
@@ -730,7 +738,7 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
                 "lag-GEMM prep");
     g_launches.fetch_add(1);
     const long long nblk = lag_blocks(n_events);
-    const int chunks = (int)(nblk < kHostChunks ? nblk : kHostChunks);
+    const int chunks = (int)(nblk < host_chunks() ? nblk : host_chunks());
     float *hv[2] = {vals_pos, vals_neg};
     int *hl[2] = {lags_pos, lags_neg};
     float *dv[2] = {d_vp, d_vn};
@@ -779,7 +787,7 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
     if (s) return s;
     const PairBandPlan bp = job_band_plan(job, d_ws);
     const long long bands = band_count(bp.nb, bp.band);
-    const int chunks = (int)(bands < kHostChunks ? bands : kHostChunks);
+    const int chunks = (int)(bands < host_chunks() ? bands : host_chunks());
     if (!st->copy_stream)
       SEISMIC_TRY(cudaStreamCreateWithFlags(&st->copy_stream, cudaStreamNonBlocking), "copy stream");
     std::vector<cudaEvent_t> done(chunks > 0 ? chunks : 0, nullptr);
