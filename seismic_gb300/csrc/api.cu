@@ -365,8 +365,7 @@ static PairBandPlan pair_band_plan(int P, const void *spectra, int stype, long l
   a.tile = tune_lookup(P, C).tile;
   PairBandPlan b{};
   if (staged_supported(P, a)) {
-    b.tile_side = staged_tile_side(P, a);
-    b.items_per_tile = b.tile_side;
+    staged_tiling(P, a, &b.tile_side, &b.items_per_tile);
   } else {
     b.tile_side = a.tile;
     b.items_per_tile = (long long)a.tile * a.tile / 2;

@@ -294,7 +294,7 @@ extern "C" int seismic_autotune(int padded_size, int n_channels, const char *cac
 
   // the staged form's CTA shape (FFT warps per CTA x chunks per ring slot)
   if (P >= 512 && P <= 4096 && staged_enabled()) {
-    const int shapes[3][2] = {{12, 4}, {12, 2}, {99, 2}};  // 99: the widest CTA of this P
+    const int shapes[4][2] = {{12, 4}, {12, 2}, {99, 4}, {99, 2}};  // 99: the widest CTA of this P
     double best_staged = 1e30;
     for (const auto &sh : shapes) {
       PairArgs sa2 = pa;

@@ -127,6 +127,13 @@ struct PairArgs {
   // candidates (FFT warps per CTA, chunks per ring slot; 0 = not forced).
   int staged_warps;
   int staged_ru;
+  // Staged form, set by its launch: i and j events per work item (TI, TJ;
+  // see StagedGeom), ceil(2^16 / (TJ / 2)) so that a group's item row is
+  // (group * item_magic) >> 16, and the bytes of one ring slot.
+  int item_i;
+  int item_j;
+  unsigned item_magic;
+  unsigned unit_bytes;
   // Poll limit of the staged form's producer waits (0: the built-in limit,
   // seconds of back-off).  Set from SEISMIC_DEVICE_WAIT_POLLS: a few polls
   // make the waits run out on a healthy GPU, which is how the abort path and
@@ -191,7 +198,8 @@ bool staged_supported(int P, const PairArgs &a);
 // and the driver's tensor-map encoder is available).
 bool staged_enabled();
 long long staged_items_total(int P, const PairArgs &a);  // triangle or rectangle
-int staged_tile_side(int P, const PairArgs &a);         // T: events per tile side (items per tile)
+// Triangle walk of the staged form: events per tile side and work items per tile.
+void staged_tiling(int P, const PairArgs &a, long long *tile_side, long long *items_per_tile);
 // Launches items [a.couple_begin, a.couple_end) of the staged decomposition.
 cudaError_t launch_pairs_staged(int P, const PairArgs &a, int sm_count, cudaStream_t s);
 

@@ -5,28 +5,31 @@
 //   inverseFFT                 Correlation_in_OMP/correlation_c.cpp:58-137
 //   the dynamic row loop       Correlation_in_OMP/correlation_c.cpp:251-293
 //
-// Work item = one event i and a block of T = 2 NG consecutive events
-// j0 .. j0+T-1; group g of the CTA's NG FFT groups takes the couple
-// (i; j0+2g, j0+2g+1) -- the same couples as the direct form, so both forms
-// give bit-identical results.  The items of the upper triangle are square
-// tiles of T x T events (T items per tile, one per i), walked in row bands
-// of `band_tiles` tile rows so the i spectra of a band stay in L2 while
-// every column to its right passes over it once (and a band's outputs are
-// contiguous packed rows); the rectangle (query x catalog) walks column
-// blocks, all queries per block.
+// Work item = TI consecutive events i0 .. i0+TI-1 and TJ = 2 NG / TI
+// consecutive events j0 .. j0+TJ-1 (StagedGeom); group g of the CTA's NG FFT
+// groups takes the couple (i0 + g / (TJ/2); j0 + 2 (g % (TJ/2)), +1) -- the
+// same couples as the direct form, so both forms give bit-identical results.
+// The items of the upper triangle tile squares of TS = lcm(TI, TJ) events,
+// walked in row bands of `band_tiles` tile rows so the i spectra of a band
+// stay in L2 while every column to its right passes over it once (and a
+// band's outputs are contiguous packed rows); the rectangle (query x
+// catalog) walks column blocks of TJ events, all query blocks per column
+// block.
 //
 // Pipeline.  Each item's spectra are cut into units (channel c, chunk r):
-// bins [r S, (r+1) S) of row i and of the T rows j0..j0+T-1, exactly the
+// bins [r S, (r+1) S) of the TI rows i0.. and the TJ rows j0.., exactly the
 // bins ca + r S and cb + r S every FFT thread reads at step r
 // (pair_core.cuh).  A producer warp (one elected thread) streams units into
-// a ring of K shared-memory slots: a 1-D bulk copy for row i's chunk and one
-// 3-D TMA box {S bins, 1 channel, T events} for the j rows (rows past the
-// catalog are zero-filled by the TMA unit), completing on the slot's `full`
-// mbarrier; the FFT warps conj-multiply from the slot and release it on its
-// `empty` mbarrier.  While the groups run their inverse FFTs the producer
-// fills the ring with the next item's first units, so spectra reads leave
-// the critical path.  Row i is staged once per unit for all NG groups:
-// 1 + T rows per T pairs instead of 3 rows per 2.
+// a ring of K shared-memory slots: two 3-D TMA boxes {S bins, 1 channel, TI
+// or TJ events} (rows past the last event are zero-filled by the TMA unit),
+// completing on the slot's `full` mbarrier; the FFT warps conj-multiply
+// from the slot and release it on its `empty` mbarrier.  While the groups
+// run their inverse FFTs the producer fills the ring with the next item's
+// units, so spectra reads leave the critical path.  A unit stages TI + TJ
+// rows for TI TJ pairs, each row shared by all the groups that use it: with
+// 24 groups, TI = 6 stages 14 rows per 48 pairs where one i per item (TI =
+// 1) stages 49, so the ring holds a whole item of the overlap-save form and
+// the FFT threads no longer wait for units at the start of an item.
 //
 // Bounded waits and the abort path.  The producer's waits (for a slot to be
 // released) are bounded by PairArgs::wait_limit polls; one that runs out sets
@@ -59,8 +62,6 @@ constexpr size_t kStagedSmemBudget = 227 * 1024;
 template <int P, int NWARP, int RU> struct Staged {  // RU: chunks r per ring slot
   static constexpr int G = P / 32;
   static constexpr int NG = NWARP * 32 / G;  // FFT groups per CTA
-  static constexpr int T = 2 * NG;           // j events per item = tile side; T items per tile
-  static constexpr int ROWS = 1 + T;         // staged rows per unit: i, j0 .. j0+T-1
   static constexpr int S = P / 16;
   static constexpr int NW = (G + 31) / 32;
   static constexpr int CONSUMERS = NWARP * 32;  // FFT threads
@@ -72,27 +73,53 @@ template <int P, int NWARP, int RU> struct Staged {  // RU: chunks r per ring sl
   // item ring of kItemRing (i, j0)
   static constexpr size_t ITEMS_OFF = PROD_OFF + 64;
   static constexpr size_t RING_OFF = (ITEMS_OFF + kItemRing * 16 + 127) / 128 * 128;
-  // one chunk r of every staged row, and a ring slot of RU chunks
-  template <int ST> static constexpr size_t sub_bytes() { return (size_t)ROWS * S * sizeof(typename SpecT<ST>::T); }
-  template <int ST> static constexpr size_t unit_bytes() { return RU * sub_bytes<ST>(); }
 };
 
-// Item w -> (i, j0).  Triangle: tile x = w / T in band order, i = bi T + w % T.
-__host__ __device__ __forceinline__ void staged_decode(const PairArgs &a, int T, long long w, long long &i,
-                                                       long long &j0) {
+// Item geometry: TI i events x TJ = 2 NG / TI j events per item (TI divides
+// NG), square tiles of TS = lcm(TI, TJ) events holding (TS / TI) x (TS / TJ)
+// items, row-major.  TI = 1 is one i per item (TS = TJ = 2 NG).
+struct StagedGeom {
+  int ti, tj, ts;
+  int jpt;        // items along a tile row: TS / TJ
+  long long ipt;  // items per tile
+};
+__host__ __device__ __forceinline__ StagedGeom staged_geom(int ng, int ti) {
+  StagedGeom g;
+  g.ti = ti;
+  g.tj = 2 * ng / ti;
+  int x = g.ti, y = g.tj;  // gcd
+  while (y) {
+    const int r = x % y;
+    x = y;
+    y = r;
+  }
+  g.ts = g.ti / x * g.tj;
+  g.jpt = g.ts / g.tj;
+  g.ipt = (long long)(g.ts / g.ti) * g.jpt;
+  return g;
+}
+
+// Item w -> (i0, j0).  Triangle: tile x = w / ipt in band order, item k =
+// w % ipt at row k / jpt, column k % jpt of the tile's items.  Rectangle:
+// column block w / ceil(n_query / TI), query block w % that.
+__host__ __device__ __forceinline__ void staged_decode(const PairArgs &a, const StagedGeom &gm, long long w,
+                                                       long long &i0, long long &j0) {
   if (a.rect) {
-    const long long blk = (w < 0x7fffffffLL && a.n_query < 0x7fffffffLL)
-                              ? (long long)((unsigned)w / (unsigned)a.n_query) : w / a.n_query;
-    i = w - blk * a.n_query;
-    j0 = a.col_begin + blk * T;
+    const long long nqb = (a.n_query + gm.ti - 1) / gm.ti;
+    const long long blk = (w < 0x7fffffffLL && nqb < 0x7fffffffLL)
+                              ? (long long)((unsigned)w / (unsigned)nqb) : w / nqb;
+    i0 = (w - blk * nqb) * gm.ti;
+    j0 = a.col_begin + blk * gm.tj;
     return;
   }
-  const long long nb = (a.n_events + T - 1) / T;
-  const long long x = w / T;
+  const long long nb = (a.n_events + gm.ts - 1) / gm.ts;
+  // 32-bit division when it fits (a 64-bit one is a long software routine)
+  const long long x = (w < 0x7fffffffLL) ? (long long)((unsigned)w / (unsigned)gm.ipt) : w / gm.ipt;
+  const int k = (int)(w - x * gm.ipt);
   long long bi, bj;
   band_tile(x, nb, a.band_tiles, bi, bj);
-  i = bi * T + (w - x * T);
-  j0 = bj * T;
+  i0 = bi * gm.ts + (long long)(k / gm.jpt) * gm.ti;
+  j0 = bj * gm.ts + (long long)(k % gm.jpt) * gm.tj;
 }
 
 // Producer side: bounded wait; on running out it raises the abort and error flags.
@@ -130,23 +157,21 @@ struct StagedItem {
 };
 
 template <int P, int NWARP, int RU, int ST>
-__device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMap *jmap, StagedCursor *cur,
-                                             StagedItem *items, unsigned char *dst, uint64_t *full) {
+__device__ __forceinline__ void staged_issue(const PairArgs &a, const StagedGeom &gm, const CUtensorMap *imap,
+                                             const CUtensorMap *jmap, StagedCursor *cur, StagedItem *items,
+                                             unsigned char *dst, uint64_t *full, uint32_t sub_bytes) {
   using SH = Staged<P, NWARP, RU>;
   using ST_T = typename SpecT<ST>::T;
-  constexpr int S = SH::S, H = P / 2;
-  constexpr uint32_t CHUNK = (uint32_t)(S * sizeof(ST_T));
+  constexpr int S = SH::S;
+  const uint32_t ibytes = (uint32_t)(gm.ti * S * sizeof(ST_T));
   const int C = spectrum_rows(a);
-  const ST_T *spec_i = reinterpret_cast<const ST_T *>(a.spectra_i ? a.spectra_i : (a.rect ? a.spectra_q : a.spectra));
-  const long long n_i = a.rect ? a.n_query : a.n_events;
-  const long long i = cur->i < n_i ? cur->i : n_i - 1;  // ragged last tile row: staged but unused
   const int c = cur->c, r = cur->r;
-  tc::mbar_arrive_expect_tx(full, (uint32_t)SH::template unit_bytes<ST>());
+  tc::mbar_arrive_expect_tx(full, RU * sub_bytes);
 #pragma unroll
   for (int h = 0; h < RU; ++h) {
-    unsigned char *d = dst + h * SH::template sub_bytes<ST>();
-    tc::bulk_load(d, spec_i + (i * C + c) * (long long)H + (r + h) * S, CHUNK, full);
-    tc::tma_load_3d(d + CHUNK, jmap, (r + h) * S, c, (int)cur->j0, full);
+    unsigned char *d = dst + h * sub_bytes;
+    tc::tma_load_3d(d, imap, (r + h) * S, c, (int)cur->i, full);
+    tc::tma_load_3d(d + ibytes, jmap, (r + h) * S, c, (int)cur->j0, full);
   }
   cur->r += RU;
   if (cur->r == 8) {
@@ -155,7 +180,7 @@ __device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMa
       cur->c = 0;
       cur->w += gridDim.x;
       if (cur->w < a.couple_end) {
-        staged_decode(a, SH::T, cur->w, cur->i, cur->j0);
+        staged_decode(a, gm, cur->w, cur->i, cur->j0);
         // published before the item's first unit is armed: that arrive
         // releases it to the FFT threads that wait on the unit
         items[++cur->seq % kItemRing] = StagedItem{cur->i, cur->j0};
@@ -166,11 +191,14 @@ __device__ __forceinline__ void staged_issue(const PairArgs &a, const CUtensorMa
 
 template <int P, int NWARP, int RU, int ST>
 __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
-    staged_pair_kernel(const PairArgs a, const __grid_constant__ CUtensorMap jmap) {
+    staged_pair_kernel(const PairArgs a, const __grid_constant__ CUtensorMap jmap,
+                       const __grid_constant__ CUtensorMap imap) {
   using SH = Staged<P, NWARP, RU>;
   using ST_T = typename SpecT<ST>::T;
-  constexpr int G = SH::G, T = SH::T, S = SH::S, NW = SH::NW;
-  constexpr uint32_t UNIT = (uint32_t)SH::template unit_bytes<ST>();
+  constexpr int G = SH::G, S = SH::S, NW = SH::NW;
+  // per-item constants come from the kernel parameters (PairArgs::item_*),
+  // not registers held across the FFT
+  const uint32_t UNIT = a.unit_bytes;
 
   extern __shared__ __align__(128) unsigned char smem[];
   float2 *bufs = reinterpret_cast<float2 *>(smem);
@@ -205,12 +233,14 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
   if (threadIdx.x >= SH::CONSUMERS) {
     // ------------------------------------------------------------ producer
     if (threadIdx.x == SH::CONSUMERS) {
+      const StagedGeom gm = staged_geom(SH::NG, a.item_i);
+      const uint32_t sub_bytes = UNIT / RU;
       const long long units_total =
           ((a.couple_end - a.couple_begin - blockIdx.x + gridDim.x - 1) / gridDim.x) * C * (8 / RU);
       cur->w = a.couple_begin + blockIdx.x;
       cur->c = 0;
       cur->r = 0;
-      staged_decode(a, T, cur->w, cur->i, cur->j0);
+      staged_decode(a, gm, cur->w, cur->i, cur->j0);
       cur->seq = 0;
       items[0] = StagedItem{cur->i, cur->j0};
       int slot = 0;
@@ -221,7 +251,8 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       const bool probed = a.wait_probe && !producer_wait(probe, 0, limit, s_abort, a.error_flag);
       for (long long u = 0; u < units_total && !probed; ++u) {
         if (u >= K && !producer_wait(&empty[slot], phase ^ 1u, limit, s_abort, a.error_flag)) break;
-        staged_issue<P, NWARP, RU, ST>(a, &jmap, cur, items, ring + (size_t)slot * UNIT, &full[slot]);
+        staged_issue<P, NWARP, RU, ST>(a, gm, &imap, &jmap, cur, items, ring + (size_t)slot * UNIT, &full[slot],
+                                       sub_bytes);
         ++issued;
         if (++slot == K) {
           slot = 0;
@@ -258,8 +289,11 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       // memory with it before the group's vote after the unit loop
       bool stop = !consumer_wait(&full[slot], phase, s_abort);
       const StagedItem it = items[seq % kItemRing];
-      const long long i = it.i, j0 = it.j0;
-      long long ja = j0 + 2 * g, jb = ja + 1;
+      // the group's i row gi and couple column gc within the item
+      const int gi = (int)(((unsigned)g * a.item_magic) >> 16), gc = g - gi * (a.item_j >> 1);
+      const int ri = gi * S, rows = a.item_i + a.item_j;
+      const long long i = it.i + gi, j0 = it.j0;
+      long long ja = j0 + 2 * gc, jb = ja + 1;
       bool live, out_b;
       if (!a.rect) {
         const bool v1 = i < N && ja < N && ja >= i;
@@ -269,11 +303,11 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
         if (!v1) ja = jb;
         if (jb >= N) jb = ja;
       } else {
-        live = ja - a.col_begin < a.n_cols;
+        live = i < a.n_query && ja - a.col_begin < a.n_cols;
         out_b = jb - a.col_begin < a.n_cols;
         if (!out_b) jb = ja;
       }
-      const int ra = (1 + (int)(ja - j0)) * S, rb = (1 + (int)(jb - j0)) * S;  // rows of ja, jb in a unit
+      const int ra = (a.item_i + (int)(ja - j0)) * S, rb = (a.item_i + (int)(jb - j0)) * S;  // rows of ja, jb in a chunk
       CoupleAcc y;
       y.zero();
       for (int c = 0; c < C && !stop; ++c) {
@@ -286,8 +320,9 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
           const ST_T *u = reinterpret_cast<const ST_T *>(ring + (size_t)slot * UNIT);
 #pragma unroll
           for (int h = 0; h < RU; ++h) {
-            const ST_T *uh = u + h * (SH::ROWS * S);
-            if (live) y.add<ST>(rp + h, uh[ca], uh[ra + ca], uh[rb + ca], uh[cb], uh[ra + cb], uh[rb + cb]);
+            const ST_T *uh = u + h * (rows * S);
+            if (live)
+              y.add<ST>(rp + h, uh[ri + ca], uh[ra + ca], uh[rb + ca], uh[ri + cb], uh[ra + cb], uh[rb + cb]);
           }
           tc::mbar_arrive(&empty[slot]);
           if (++slot == K) {
@@ -333,14 +368,17 @@ constexpr int kStagedWarps = 12;  // FFT warps per CTA, plus the producer warp
 constexpr int staged_wide_warps(int P) { return P >= 4096 ? 12 : (P == 2048 ? 14 : 15); }
 
 // CTA shape of a launch: FFT warps per CTA and chunks per ring slot.  In
-// order: a shape the autotuner forces while timing, SEISMIC_STAGED_WARPS /
-// SEISMIC_STAGED_RU, the tuner's cached choice for exactly (P, spectrum
-// rows), else the built-in rule: the wide CTA (more FFT warps, a smaller
-// ring) where one spectrum row's item fits it -- one channel at P = 2048
-// (FP32 spectra 263 vs 230 M pairs/s measured, FP16 256 vs 233, BF16 255 vs
-// 237; with three channels 175 vs 184) -- and 4-chunk slots otherwise.  The
-// wide FP32 CTA has room for 2-chunk slots only; half-precision spectra
-// always take 4.
+// order: a shape the autotuner forces while timing, SEISMIC_STAGED_WARPS
+// ("12", "wide") / SEISMIC_STAGED_RU ("2", "4"), the tuner's cached choice
+// for exactly (P, spectrum rows), else the built-in rule: the wide CTA (the
+// most FFT warps that keep 128 registers a thread) with 4-chunk slots.
+// Measured with items of TI x TJ events, FP32, M pairs/s, 12 warps / wide:
+// overlap-save Q=512 x 4 rows 710 / 825, Q=1024 x 2 rows 451 / 516, P=512
+// one channel 977 / 1128, P=1024 523 / 585, P=1024 three channels 380 /
+// 469, P=2048 219 / 274, P=2048 three channels 192 / 195 (P=4096: the same
+// CTA).  Half-precision spectra always take 4-chunk slots; an FP32 launch
+// whose item rows leave no room for two 4-chunk slots takes 2
+// (launch_staged_p).
 struct StagedShape {
   int nwarp, ru;
 };
@@ -355,17 +393,16 @@ static StagedShape staged_shape(int P, const PairArgs &a) {
   if (!ru) {
     const char *e = getenv("SEISMIC_STAGED_RU");
     if (e && strcmp(e, "2") == 0) ru = 2;
+    if (e && strcmp(e, "4") == 0) ru = 4;
   }
   int tw = 0, tru = 0;
   if ((!w || !ru) && tune_staged_lookup(P, rows, &tw, &tru)) {
     if (!w) w = tw;
     if (!ru) ru = tru;
   }
-  if (!w) w = (P == 2048 && rows == 1) ? staged_wide_warps(P) : kStagedWarps;
+  if (!w) w = staged_wide_warps(P);
   w = (w == kStagedWarps) ? kStagedWarps : staged_wide_warps(P);
-  if (a.stype != 0) ru = 4;                       // half spectra: 4-chunk slots
-  else if (w != kStagedWarps) ru = 2;             // the wide FP32 CTA: 2-chunk slots
-  else ru = (ru == 2) ? 2 : 4;
+  ru = (a.stype != 0 || ru != 2) ? 4 : 2;
   return StagedShape{w, ru};
 }
 
@@ -385,13 +422,59 @@ bool staged_supported(int P, const PairArgs &a) {
   return tensor_map_encoder() != nullptr;
 }
 
-int staged_tile_side(int P, const PairArgs &a) { return 2 * (staged_shape(P, a).nwarp * 32 / (P / 32)); }
+// i events per item (TI, a divisor of the NG groups): SEISMIC_STAGED_TI if it
+// divides NG, else the fewest staged rows TI + 2 NG / TI per unit -- on the
+// rectangle among the TI that cover the queries with the fewest padding rows
+// (a one-query request keeps TI = 1).
+static int staged_item_rows(int ng, const PairArgs &a) {
+  if (const char *e = getenv("SEISMIC_STAGED_TI")) {
+    const int v = atoi(e);
+    if (v >= 1 && v <= ng && ng % v == 0) return v;
+  }
+  int best = 1, best_rows = 0;
+  long long best_pad = -1;
+  for (int d = 1; d <= ng; ++d) {
+    if (ng % d) continue;
+    const int rows = d + 2 * ng / d;
+    const long long pad = a.rect ? (a.n_query + d - 1) / d * d - a.n_query : 0;
+    if (best_pad < 0 || pad < best_pad || (pad == best_pad && rows < best_rows)) {
+      best = d;
+      best_rows = rows;
+      best_pad = pad;
+    }
+  }
+  return best;
+}
+
+static StagedGeom staged_geom_of(int P, const PairArgs &a) {
+  const int ng = staged_shape(P, a).nwarp * 32 / (P / 32);
+  return staged_geom(ng, staged_item_rows(ng, a));
+}
+
+void staged_tiling(int P, const PairArgs &a, long long *tile_side, long long *items_per_tile) {
+  const StagedGeom gm = staged_geom_of(P, a);
+  *tile_side = gm.ts;
+  *items_per_tile = gm.ipt;
+}
 
 long long staged_items_total(int P, const PairArgs &a) {
-  const long long T = staged_tile_side(P, a);
-  if (a.rect) return a.n_query * ((a.n_cols + T - 1) / T);
-  const long long nb = (a.n_events + T - 1) / T;
-  return T * (nb * (nb + 1) / 2);
+  const StagedGeom gm = staged_geom_of(P, a);
+  if (a.rect) return (a.n_query + gm.ti - 1) / gm.ti * ((a.n_cols + gm.tj - 1) / gm.tj);
+  const long long nb = (a.n_events + gm.ts - 1) / gm.ts;
+  return gm.ipt * (nb * (nb + 1) / 2);
+}
+
+// Ring slots of a launch: the shared memory left beside the FFT exchange
+// buffers (and room for the largest shared histogram), in slots of RU chunks
+// of the item's TI + TJ rows; at most kStagedRingMax.
+template <int P, int NWARP, int RU, int ST> static int staged_ring_slots(const PairArgs &a, size_t *unit_bytes) {
+  using SH = Staged<P, NWARP, RU>;
+  const StagedGeom gm = staged_geom(SH::NG, staged_item_rows(SH::NG, a));
+  const size_t unit = (size_t)RU * (gm.ti + gm.tj) * SH::S * sizeof(typename SpecT<ST>::T);
+  if (unit_bytes) *unit_bytes = unit;
+  const size_t hist_reserve = (size_t)2 * kStagedHistMax * sizeof(int);
+  const int K = (int)((kStagedSmemBudget - SH::RING_OFF - hist_reserve) / (unit + 2 * sizeof(uint64_t)));
+  return K > kStagedRingMax ? kStagedRingMax : K;
 }
 
 template <int P, int NWARP, int RU, int ST>
@@ -399,10 +482,14 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
   using SH = Staged<P, NWARP, RU>;
   using ST_T = typename SpecT<ST>::T;
   PairArgs a = a0;
-  const size_t unit = SH::template unit_bytes<ST>();
-  const size_t hist_reserve = (size_t)2 * kStagedHistMax * sizeof(int);
-  int K = (int)((kStagedSmemBudget - SH::RING_OFF - hist_reserve) / (unit + 2 * sizeof(uint64_t)));
-  if (K > kStagedRingMax) K = kStagedRingMax;
+  a.item_i = staged_item_rows(SH::NG, a);
+  const StagedGeom gm = staged_geom(SH::NG, a.item_i);
+  a.item_j = gm.tj;
+  // g / (TJ/2) = (g * ceil(2^16 / (TJ/2))) >> 16 exactly while g * TJ/2 < 2^16
+  a.item_magic = (unsigned)((65536 + gm.tj / 2 - 1) / (gm.tj / 2));
+  size_t unit = 0;
+  const int K = staged_ring_slots<P, NWARP, RU, ST>(a, &unit);
+  a.unit_bytes = (unsigned)unit;
   if (K < 2) return cudaErrorInvalidConfiguration;
   a.ring = K;
   const size_t hist_bytes = (a.n_hist > 0 && a.n_hist <= kStagedHistMax) ? (size_t)2 * a.n_hist * sizeof(int) : 0;
@@ -411,38 +498,48 @@ static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_
     cudaError_t e = ensure_dynamic_smem((const void *)staged_pair_kernel<P, NWARP, RU, ST>, (int)kStagedSmemBudget);
     if (e != cudaSuccess) return e;
   }
-  a.band_tiles = l2_band_tiles(spectrum_rows(a), P, (int)sizeof(ST_T), SH::T);
+  a.band_tiles = l2_band_tiles(spectrum_rows(a), P, (int)sizeof(ST_T), gm.ts);
   a.wait_limit = device_wait_polls();
   a.wait_probe = device_wait_probe();
 
-  // Tensor map of the j spectra: dims {P/2 bins, C channels, N events},
-  // box {S bins, 1 channel, T events}.
-  CUtensorMap map;
-  const cuuint64_t dims[3] = {(cuuint64_t)(P / 2), (cuuint64_t)spectrum_rows(a), (cuuint64_t)a.n_events};
+  // Tensor maps of the j and the i spectra: dims {P/2 bins, C spectrum rows,
+  // events}, boxes {S bins, 1 row, TJ or TI events}.
+  CUtensorMap map, imap;
+  const void *spec_i = a.spectra_i ? a.spectra_i : (a.rect ? a.spectra_q : a.spectra);
+  const long long n_i = a.rect ? a.n_query : a.n_events;
   const cuuint64_t strides[2] = {(cuuint64_t)(P / 2) * sizeof(ST_T),
                                  (cuuint64_t)spectrum_rows(a) * (P / 2) * sizeof(ST_T)};
-  const cuuint32_t box[3] = {(cuuint32_t)SH::S, 1u, (cuuint32_t)SH::T};
   const cuuint32_t estr[3] = {1, 1, 1};
   const CUtensorMapDataType dt = sizeof(ST_T) == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
-  if (tensor_map_encoder()(&map, dt, 3, const_cast<void *>(a.spectra), dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-    return cudaErrorInvalidValue;
+  for (int side = 0; side < 2; ++side) {
+    const cuuint64_t dims[3] = {(cuuint64_t)(P / 2), (cuuint64_t)spectrum_rows(a),
+                                (cuuint64_t)(side == 0 ? a.n_events : n_i)};
+    const cuuint32_t box[3] = {(cuuint32_t)SH::S, 1u, (cuuint32_t)(side == 0 ? gm.tj : gm.ti)};
+    if (tensor_map_encoder()(side == 0 ? &map : &imap, dt, 3, const_cast<void *>(side == 0 ? a.spectra : spec_i),
+                             dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorInvalidValue;
+  }
   const long long items = a.couple_end - a.couple_begin;
   if (items <= 0) return cudaSuccess;
   const int grid = (int)(items < sm_count ? items : sm_count);
-  staged_pair_kernel<P, NWARP, RU, ST><<<grid, SH::THREADS, smem, s>>>(a, map);
+  staged_pair_kernel<P, NWARP, RU, ST><<<grid, SH::THREADS, smem, s>>>(a, map, imap);
   return cudaGetLastError();
 }
 
 template <int P> static cudaError_t launch_staged_p(const PairArgs &a, int sm_count, cudaStream_t s) {
   const StagedShape sh = staged_shape(P, a);
   const bool wide = sh.nwarp != kStagedWarps;
+  constexpr int WW = staged_wide_warps(P);
   switch (a.stype) {
     case 0:
-      if (wide) return launch_staged_t<P, staged_wide_warps(P), 2, 0>(a, sm_count, s);
-      return sh.ru == 2 ? launch_staged_t<P, kStagedWarps, 2, 0>(a, sm_count, s)
-                        : launch_staged_t<P, kStagedWarps, 4, 0>(a, sm_count, s);
+      if (wide)
+        return (sh.ru == 4 && staged_ring_slots<P, WW, 4, 0>(a, nullptr) >= 2)
+                   ? launch_staged_t<P, WW, 4, 0>(a, sm_count, s)
+                   : launch_staged_t<P, WW, 2, 0>(a, sm_count, s);
+      return (sh.ru == 4 && staged_ring_slots<P, kStagedWarps, 4, 0>(a, nullptr) >= 2)
+                 ? launch_staged_t<P, kStagedWarps, 4, 0>(a, sm_count, s)
+                 : launch_staged_t<P, kStagedWarps, 2, 0>(a, sm_count, s);
     case 1:
       return wide ? launch_staged_t<P, staged_wide_warps(P), 4, 1>(a, sm_count, s)
                   : launch_staged_t<P, kStagedWarps, 4, 1>(a, sm_count, s);

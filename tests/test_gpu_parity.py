@@ -244,6 +244,38 @@ def test_staged_and_direct_forms_agree_bitwise(cuda_ok, monkeypatch, n, c, lengt
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("n,c,length,shift,block", [
+    (203, 1, 1024, 128, "on"),    # overlap-save frames Q = 512 x 4: 24 groups, TI = 6
+    (150, 3, 700, 300, "off"),    # P = 1024, ragged last tile: 12 groups
+    (130, 3, 2048, 1500, "off"),  # P = 4096: 3 groups, TI = 3
+    (90, 1, 1024, 128, "off"),    # P = 2048, the wide CTA: 7 groups, TI = 7
+])
+def test_staged_item_shapes_agree_bitwise(cuda_ok, monkeypatch, n, c, length, shift, block):
+    """Staged work items of TI i events x TJ j events -- the automatic TI,
+    one i per item, and other divisors of the group count -- run the same
+    couples in the same arithmetic: identical outputs and histograms, and
+    the automatic one within the FP64 bar."""
+    import torch
+    ev = synth.family_catalog(n, c, length, n_families=max(1, n // 10), seed=n + 3 * c)
+    t = torch.from_numpy(ev).cuda()
+    monkeypatch.setenv("SEISMIC_BLOCK_FORM", block)
+    got = {}
+    for ti in ("", "1", "2", "3"):
+        monkeypatch.setenv("SEISMIC_STAGED_TI", ti)
+        r = xcorr.xcorr(t, shift, threshold=0.0, n_classes_hist=16)
+        torch.cuda.synchronize()
+        got[ti] = [x.cpu().numpy() for x in (r.vals_pos, r.lags_pos, r.vals_neg, r.lags_neg)] + \
+                  [r.max_hist.cpu().numpy(), r.min_hist.cpu().numpy()]
+    i, j = O.triu_pairs(n)
+    ref = O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(length, shift))
+    ag = O.agreement(*got[""][:4], ref)
+    assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, ag
+    assert ag.lag_mismatch == 0, ag
+    for ti in ("1", "2", "3"):
+        for a, b in zip(got[""], got[ti]):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_precision_workload_size_properties(cuda_ok):
     """Full-size N=16384, L=1024, +-128 lags: properties that hold at any size
     (diagonal coefficient 1 at lag 0, |coef| <= 1, histogram totals) and an

@@ -46,6 +46,25 @@ def test_server_results_vs_fp64(cuda_ok, form, tol):
     srv.close()
 
 
+def test_server_item_shapes_agree_bitwise(cuda_ok, monkeypatch):
+    """Rectangle work items of TI queries x TJ catalog events: TI = 1, 2 and
+    3 over a 7-event request (query blocks padded past the last query) give
+    the same results bit for bit."""
+    from seismic_gb300.serving import Server
+    cat = _catalog()
+    query = synth.family_catalog(7, 3, 512, n_families=2, seed=74)
+    got = {}
+    for ti in ("1", "2", "3"):
+        monkeypatch.setenv("SEISMIC_STAGED_TI", ti)
+        srv = Server(cat, shift=100, form="fp32", n_slots=2, max_query_events=8, topk=4)
+        res = srv.wait(srv.submit(query, subset=(3, 557)))
+        got[ti] = [res.vals_pos, res.lags_pos, res.vals_neg, res.lags_neg, res.topk_index]
+        srv.close()
+    for ti in ("2", "3"):
+        for a, b in zip(got["1"], got[ti]):
+            np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("form", ["fp16", "laggemm16"])
 def test_server_same_result_alone_and_in_the_mix(cuda_ok, form):
     """A request gives bit-identical results alone and when it is admitted
