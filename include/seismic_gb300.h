@@ -111,8 +111,11 @@ const char *seismic_status_string(int status);
 
 /* Padded FFT size used when a native call passes padded_size = 0: the
  * smallest power of two >= event_length + shift (exact linear correlation
- * over the whole lag window).  Returns 0 if that exceeds the supported
- * maximum (8192). */
+ * over the whole lag window).  Supported: up to 16384 (the plain transform),
+ * and beyond, up to 2^24, where shift <= 1792 (the FFT forms then run the
+ * overlap-save form, the same linear correlation).  Returns 0 otherwise.
+ * Batched catalogs and the entry points given precomputed spectra take the
+ * plain sizes only (batched: up to 8192). */
 int seismic_resolve_padded_size(int event_length, int shift);
 
 /* Device workspace (bytes) seismic_xcorr_device needs for these sizes

@@ -140,11 +140,13 @@ static size_t norms_bytes(long long rows) { return norms_buffer_bytes(rows); }
 // Overlap-save plan of a short lag window (declared in kernels.cuh).  The
 // pair cost of a transform size is its inverse FFT plus the conj-products
 // of every spectrum row, 2.5 Q log2 Q + 6 C nb (Q/2) flop per pair; a block
-// form is chosen when it costs under 3/4 of the plain size-P form.  Only
-// where the plain form has no circular aliasing (L + shift <= P), so both
-// compute the same linear correlation, and only for the sizes of the staged
-// pair form (it has no direct-load twin).  SEISMIC_BLOCK_FORM=off keeps the
-// plain form.
+// form is chosen when it costs under 3/4 of the plain size-P form, and
+// always (the cheapest Q) for a padded size beyond the plain transform's
+// kMaxP, which has no other form.  Only where the plain form has no circular
+// aliasing (L + shift <= P), so both compute the same linear correlation,
+// and only for the sizes of the staged pair form (it has no direct-load
+// twin).  SEISMIC_BLOCK_FORM=off keeps the plain form (padded sizes up to
+// kMaxP).
 BlockPlan block_plan(int length, int shift, int P, int n_channels, int stype) {
   BlockPlan best;
   const char *env = getenv("SEISMIC_BLOCK_FORM");
@@ -155,7 +157,7 @@ BlockPlan block_plan(int length, int shift, int P, int n_channels, int stype) {
   auto cost = [&](int q, int nb) {
     return 2.5 * q * (31 - __builtin_clz((unsigned)q)) + 6.0 * n_channels * nb * (q / 2);
   };
-  double best_cost = 0.75 * cost(P, 1);
+  double best_cost = P > kMaxP ? 1e300 : 0.75 * cost(P, 1);
   for (int q = 512; q <= 4096 && q < P; q <<= 1) {
     const int b = q - 2 * shift;  // B + 2 shift <= Q
     if (b < q / 8) continue;      // blocks too short to pay for their frames
@@ -211,13 +213,27 @@ static bool is_lag_form(int form) {
   return form == SEISMIC_FORM_LAGGEMM_BF16X3 || form == SEISMIC_FORM_LAGGEMM_FP16;
 }
 
+// A padded size the FFT forms run: a power of two up to kMaxP (the plain
+// transform), or beyond it up to kMaxPadded where the overlap-save form
+// takes the lag window (unless plain_only: entry points given plain spectra).
+static bool fft_size_ok(int padded, int event_length, int shift, int n_channels, int form, bool plain_only) {
+  if (supported_padded_size(padded)) return true;
+  if (plain_only || padded <= kMaxP || padded > kMaxPadded || (padded & (padded - 1)) != 0) return false;
+  return block_plan(event_length, shift, padded, n_channels, form_stype(form)).nb > 0;
+}
+
 static int validate(long long n_events, int n_channels, int event_length, int padded, int shift,
-                    int n_hist, int form) {
+                    int n_hist, int form, bool plain_only = false) {
   if (n_events < 1) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_events must be >= 1 (got %lld)", n_events);
   if (n_channels < 1) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "n_channels must be >= 1");
   if (event_length < 1) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "event_length must be >= 1");
-  if (!supported_padded_size(padded))
-    return set_status(SEISMIC_ERR_UNSUPPORTED_SIZE, "paddedSize %d unsupported (power of two in [64, 8192])", padded);
+  if (is_lag_form(form) ? (padded < kMinP || padded > kMaxPadded || (padded & (padded - 1)) != 0)
+                        : !fft_size_ok(padded, event_length, shift, n_channels, form, plain_only))
+    return set_status(SEISMIC_ERR_UNSUPPORTED_SIZE,
+                      plain_only ? "paddedSize %d unsupported (power of two in [64, 16384])"
+                                 : "paddedSize %d unsupported (power of two in [64, 16384]; larger ones where the "
+                                   "overlap-save form takes the lag window: shift <= 1792, FP32 or FP16 spectra)",
+                      padded);
   if (event_length > padded)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "event_length %d exceeds paddedSize %d", event_length, padded);
   if (shift < 0) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "shift must be >= 0");
@@ -444,8 +460,8 @@ int report_status(int status, const char *message) { return set_status(status, "
 int report_cuda(cudaError_t e, const char *what) { return cuda_status(e, what); }
 void note_launches(unsigned n) { g_launches.fetch_add(n); }
 int check_xcorr_args(long long n_events, int n_channels, int event_length, int padded, int shift, int n_hist,
-                     int form) {
-  return validate(n_events, n_channels, event_length, padded, shift, n_hist, form);
+                     int form, bool plain_only) {
+  return validate(n_events, n_channels, event_length, padded, shift, n_hist, form, plain_only);
 }
 
 // Core: spectra + pairs on `stream`; buffers all on device.
@@ -515,7 +531,8 @@ int seismic_resolve_padded_size(int event_length, int shift) {
   long long need = (long long)event_length + shift;
   long long p = kMinP;
   while (p < need) p <<= 1;
-  return p <= kMaxP ? (int)p : 0;
+  if (p <= kMaxP) return (int)p;
+  return (p <= kMaxPadded && shift <= kMaxBlockShift) ? (int)p : 0;  // the overlap-save form's sizes
 }
 
 size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int event_length, int shift,
@@ -526,7 +543,7 @@ size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int eve
     return lag_workspace_bytes(n_events, n_channels, event_length, lag_planes(form));
   }
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
-  if (!supported_padded_size(padded_size)) return 0;
+  if (!fft_size_ok(padded_size, event_length, shift, n_channels, form, false)) return 0;
   return fft_job(n_events, n_channels, event_length, shift, padded_size, form_stype(form)).total();
 }
 
@@ -611,7 +628,7 @@ int seismic_spectra_device(const float *d_events, long long n_events, int n_chan
                            long long event_stride, long long channel_stride, int padded_size, int prescale,
                            void *d_spectra, double *d_norms, void *stream) {
   set_status(SEISMIC_OK, "");
-  int s = validate(n_events, n_channels, event_length, padded_size, 0, 0, SEISMIC_FORM_FP32);
+  int s = validate(n_events, n_channels, event_length, padded_size, 0, 0, SEISMIC_FORM_FP32, true);
   if (s) return s;
   if (!d_events || !d_spectra || !d_norms) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");
   int dev;
@@ -626,7 +643,7 @@ int seismic_pairs_device(const void *d_spectra, const double *d_norms, long long
                          float *d_vals_pos, int *d_lags_pos, float *d_vals_neg, int *d_lags_neg, int *d_max_hist,
                          int *d_min_hist, void *stream) {
   set_status(SEISMIC_OK, "");
-  int s = validate(n_events, n_channels, 1, padded_size, shift, n_classes_hist, form);
+  int s = validate(n_events, n_channels, 1, padded_size, shift, n_classes_hist, form, true);
   if (s) return s;
   if (!d_spectra || !d_norms || !d_vals_pos || !d_lags_pos || !d_vals_neg || !d_lags_neg)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");
@@ -660,7 +677,7 @@ int seismic_pairs_device_range(const void *d_spectra, const double *d_norms, lon
                                long long couple_begin, long long couple_end, float *d_vals_pos, int *d_lags_pos,
                                float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist, void *stream) {
   set_status(SEISMIC_OK, "");
-  int s = validate(n_events, n_channels, 1, padded_size, shift, n_classes_hist, SEISMIC_FORM_FP32);
+  int s = validate(n_events, n_channels, 1, padded_size, shift, n_classes_hist, SEISMIC_FORM_FP32, true);
   if (s) return s;
   if (!d_spectra || !d_norms || !d_vals_pos || !d_lags_pos || !d_vals_neg || !d_lags_neg)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");

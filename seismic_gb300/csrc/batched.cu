@@ -128,8 +128,12 @@ extern "C" int seismic_batch_create(const seismic_catalog *catalogs, int n_catal
   for (int k = 0; k < n_catalogs; ++k) {
     const seismic_catalog &c = catalogs[k];
     const int P = seismic_resolve_padded_size(c.event_length, c.shift);
-    s = check_xcorr_args(c.n_events, c.n_channels, c.event_length, P, c.shift, c.n_classes_hist, SEISMIC_FORM_FP32);
+    s = check_xcorr_args(c.n_events, c.n_channels, c.event_length, P, c.shift, c.n_classes_hist, SEISMIC_FORM_FP32,
+                         true);
     if (s) return s;
+    if (P > kMaxBatchP)
+      return report_status(SEISMIC_ERR_UNSUPPORTED_SIZE,
+                           "batched catalogs: padded size up to 8192 (event_length + shift <= 8192)");
     if (!c.events || !c.vals_pos || !c.lags_pos || !c.vals_neg || !c.lags_neg ||
         (c.n_classes_hist > 0 && (!c.max_hist || !c.min_hist)))
       return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "catalog with a null buffer");

@@ -33,6 +33,7 @@ template <> struct FftPlan<1024> { static constexpr int R2 = 16, R3 = 4, R4 = 0;
 template <> struct FftPlan<2048> { static constexpr int R2 = 16, R3 = 8, R4 = 0; };
 template <> struct FftPlan<4096> { static constexpr int R2 = 16, R3 = 16, R4 = 0; };
 template <> struct FftPlan<8192> { static constexpr int R2 = 16, R3 = 8, R4 = 4; };
+template <> struct FftPlan<16384> { static constexpr int R2 = 16, R3 = 16, R4 = 4; };
 
 __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
 template <int P> __host__ __device__ constexpr int padded_len() { return P + P / 16; }

@@ -8,8 +8,11 @@
 
 namespace seismic {
 
-constexpr int kMaxP = 8192;  // largest supported padded FFT size
-constexpr int kMinP = 64;    // smallest
+constexpr int kMaxP = 16384;  // largest padded size of the plain transform (one 512-thread FFT group a CTA)
+constexpr int kMinP = 64;     // smallest
+constexpr int kMaxBatchP = 8192;          // batched launches (256-thread CTAs)
+constexpr int kMaxPadded = 1 << 24;       // beyond kMaxP: the overlap-save form only
+constexpr int kMaxBlockShift = 7 * 4096 / 16;  // its widest lag window: frames of Q = 4096, blocks >= Q / 8
 
 // Layout of the packed half spectrum of one (event, channel) row:
 //   slot 0      = (Re X[0], Re X[P/2])   (both bins are real for real input)
@@ -315,7 +318,9 @@ int pair_ctas_per_sm_cached(int P);
 int report_status(int status, const char *message);
 int report_cuda(cudaError_t e, const char *what);
 void note_launches(unsigned n);
+// plain_only: the padded size must be one of the plain transform (the caller
+// runs no overlap-save form).
 int check_xcorr_args(long long n_events, int n_channels, int event_length, int padded, int shift, int n_hist,
-                     int form);
+                     int form, bool plain_only = false);
 
 }  // namespace seismic

@@ -103,7 +103,7 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
   report_status(SEISMIC_OK, "");
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
   int s = check_xcorr_args(n_events, n_channels, event_length, padded_size, shift, n_classes_hist,
-                           SEISMIC_FORM_FP32);
+                           SEISMIC_FORM_FP32, true);
   if (s) return s;
   if (!d_events || !d_vals_pos || !d_lags_pos || !d_vals_neg || !d_lags_neg)
     return report_status(SEISMIC_ERR_INVALID_ARGUMENT, "null buffer");

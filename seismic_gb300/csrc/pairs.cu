@@ -49,8 +49,10 @@ template <int P> __device__ __forceinline__ int *pair_hist_smem(unsigned char *s
                                  (size_t)NG * NW * 8 * sizeof(unsigned));
 }
 
+// 256 threads (two CTAs per SM), or one FFT group of P/32 threads where that
+// is more (P = 16384: 512 threads, 139 KB of exchange buffer, one CTA per SM).
 template <int P, int ST>
-__global__ void __launch_bounds__(256, 2) pair_kernel(PairArgs a) {
+__global__ void __launch_bounds__((P / 32 > 256 ? P / 32 : 256), (P / 32 > 256 ? 1 : 2)) pair_kernel(PairArgs a) {
   constexpr int NG = (256 / (P / 32)) > 0 ? (256 / (P / 32)) : 1;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -380,6 +382,7 @@ int pair_ctas_per_sm(int P) {
     case 2048: return ctas_per_sm_t<2048>();
     case 4096: return ctas_per_sm_t<4096>();
     case 8192: return ctas_per_sm_t<8192>();
+    case 16384: return ctas_per_sm_t<16384>();
     default: return 1;
   }
 }
@@ -394,6 +397,7 @@ cudaError_t launch_pairs(int P, const PairArgs &a, int grid, cudaStream_t s) {
     case 2048: return launch_pairs_t<2048>(a, grid, s);
     case 4096: return launch_pairs_t<4096>(a, grid, s);
     case 8192: return launch_pairs_t<8192>(a, grid, s);
+    case 16384: return launch_pairs_t<16384>(a, grid, s);
     default: return cudaErrorInvalidValue;
   }
 }

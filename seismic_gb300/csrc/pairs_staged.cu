@@ -423,24 +423,28 @@ bool staged_supported(int P, const PairArgs &a) {
 }
 
 // i events per item (TI, a divisor of the NG groups): SEISMIC_STAGED_TI if it
-// divides NG, else the fewest staged rows TI + 2 NG / TI per unit -- on the
-// rectangle among the TI that cover the queries with the fewest padding rows
-// (a one-query request keeps TI = 1).
+// divides NG, else the TI of least estimated time per pair,
+//   (query rows covered / query rows) x (1 + 0.18 (TI + TJ) / (2 NG)):
+// the first factor is the FFT work of groups left without a query on the
+// rectangle (1 on the triangle), the second the staging of TI + TJ rows per
+// 2 NG pairs (one i per item, 49 rows per 48 pairs, measured 13 % slower than
+// 14 rows per 48 on the overlap-save form).  The triangle takes the fewest
+// rows; a one-query request keeps TI = 1.
 static int staged_item_rows(int ng, const PairArgs &a) {
   if (const char *e = getenv("SEISMIC_STAGED_TI")) {
     const int v = atoi(e);
     if (v >= 1 && v <= ng && ng % v == 0) return v;
   }
-  int best = 1, best_rows = 0;
-  long long best_pad = -1;
+  int best = 1;
+  double best_cost = 0.0;
   for (int d = 1; d <= ng; ++d) {
     if (ng % d) continue;
-    const int rows = d + 2 * ng / d;
-    const long long pad = a.rect ? (a.n_query + d - 1) / d * d - a.n_query : 0;
-    if (best_pad < 0 || pad < best_pad || (pad == best_pad && rows < best_rows)) {
+    const double rows = d + 2.0 * ng / d;
+    const double pad = (a.rect && a.n_query > 0) ? (double)((a.n_query + d - 1) / d * d) / (double)a.n_query : 1.0;
+    const double cost = pad * (1.0 + 0.18 * rows / (2.0 * ng));
+    if (d == 1 || cost < best_cost) {
       best = d;
-      best_rows = rows;
-      best_pad = pad;
+      best_cost = cost;
     }
   }
   return best;

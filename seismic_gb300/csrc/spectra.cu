@@ -98,7 +98,7 @@ template <int P> __device__ __forceinline__ void spectra_body(const SpectraArgs 
                                                               unsigned char *smem_raw);
 
 template <int P>
-__global__ void __launch_bounds__(256) spectra_kernel(SpectraArgs a) {
+__global__ void __launch_bounds__(P / 32 > 256 ? P / 32 : 256) spectra_kernel(SpectraArgs a) {
   constexpr int G = P / 32;
   constexpr int NG = (256 / G) > 0 ? (256 / G) : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -299,6 +299,7 @@ cudaError_t launch_spectra(int P, const SpectraArgs &a, cudaStream_t s) {
     case 2048: return launch_spectra_t<2048>(a, s);
     case 4096: return launch_spectra_t<4096>(a, s);
     case 8192: return launch_spectra_t<8192>(a, s);
+    case 16384: return launch_spectra_t<16384>(a, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -10,7 +10,7 @@ import pytest
 
 from conftest import golden_cases, load_golden
 from oracle import oracle as O
-from seismic_gb300 import correlation_lib, synth, xcorr
+from seismic_gb300 import _lib, correlation_lib, synth, xcorr
 from tolerances import check_hist, check_pairs
 
 pytestmark = pytest.mark.gpu
@@ -104,6 +104,8 @@ def test_small_workload_full_triangle_vs_port(cuda_ok):
     (11, 32, 32, 0.0, 4),          # P = 64
     (21, 200, 56, 0.1, 6),         # P = 256
     (70, 700, 300, 0.05, 17),      # P = 1024, non-power-of-two L
+    (6, 9000, 9000, 0.0, 10),      # P = 16384: one 512-thread FFT group per CTA
+    (5, 17000, 300, 0.1, 8),       # padded 32768: beyond the plain transform, the overlap-save form
 ])
 def test_sizes_vs_port(cuda_ok, n, length, shift, thr, nh):
     ev = synth.family_catalog(n, 1, length, n_families=max(1, n // 4), seed=n + length)[:, 0]
@@ -113,6 +115,32 @@ def test_sizes_vs_port(cuda_ok, n, length, shift, thr, nh):
     r = O.fp64_xcorr(ev, shift, i, j)
     check_pairs(got[:4], (exp.vals_pos, exp.lags_pos, exp.vals_neg, exp.lags_neg), r, thr)
     check_hist(got[4], got[5], exp.max_hist, exp.min_hist, r, nh)
+
+
+def test_large_padded_sizes_native(cuda_ok):
+    """The native entry point on long events: P = 16384 (plain, three channels)
+    and a 2^17 padded size with a short lag window (overlap-save frames), each
+    against FP64; a padded size beyond the plain transform whose lag window
+    the overlap-save form cannot take is refused."""
+    import ctypes
+    import torch
+    lib = _lib.lib()
+    for n, c, length, shift in ((7, 3, 6000, 5000), (4, 1, 70000, 1000)):
+        ev = synth.family_catalog(n, c, length, n_families=2, seed=length)
+        r = xcorr.xcorr(torch.from_numpy(ev).cuda(), shift, threshold=0.0, n_classes_hist=8)
+        torch.cuda.synchronize()
+        P = xcorr.resolve_padded_size(length, shift)
+        i, j = O.triu_pairs(n)
+        ref = O.fp64_xcorr(ev, shift, i, j, padded=P)
+        ag = O.agreement(r.vals_pos.cpu().numpy(), r.lags_pos.cpu().numpy(), r.vals_neg.cpu().numpy(),
+                         r.lags_neg.cpu().numpy(), ref)
+        assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, (length, ag)
+        assert ag.lag_mismatch == 0, (length, ag)
+    P, nb, bl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    _lib.check(lib.seismic_fft_plan(70000, 1000, 0, 1, 0, ctypes.byref(P), ctypes.byref(nb), ctypes.byref(bl)))
+    assert nb.value > 0 and P.value <= 4096
+    assert lib.seismic_fft_plan(20000, 3000, 32768, 1, 0, ctypes.byref(P), ctypes.byref(nb), ctypes.byref(bl)) == 2
+    assert lib.seismic_xcorr_workspace_bytes(4, 1, 20000, 3000, 32768, 0) == 0
 
 
 def test_zero_norm_event_defined(cuda_ok):

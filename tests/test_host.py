@@ -31,7 +31,11 @@ def test_resolve_padded_size(built_lib):
     assert xcorr.resolve_padded_size(1024, 128) == 2048
     assert xcorr.resolve_padded_size(1000, 1000) == 2048
     assert xcorr.resolve_padded_size(3000, 3000) == 8192
-    assert xcorr.resolve_padded_size(5000, 5000) == 0
+    assert xcorr.resolve_padded_size(5000, 5000) == 16384
+    assert xcorr.resolve_padded_size(9000, 9000) == 0       # beyond the plain transform, lag window too wide
+    assert xcorr.resolve_padded_size(20000, 300) == 32768   # the overlap-save form's sizes
+    assert xcorr.resolve_padded_size(20000, 1792) == 32768
+    assert xcorr.resolve_padded_size(20000, 1793) == 0
     assert xcorr.resolve_padded_size(10, 5) == 64
 
 
