@@ -102,23 +102,30 @@ template <> struct SpecT<0> {
   }
   __device__ static __forceinline__ float2 f2(float2 a) { return a; }
 };
+// Half types: y += a conj(b) by mixed-precision FMA (16-bit factors, FP32
+// addend and result): each product of two 16-bit values is exact in FP32 and
+// is added with one rounding, in the FP32 form's order -- four FMAs, like
+// FP32, where HMUL2 products rounded every product to 16 bits and needed
+// conversions and adds besides.
 template <> struct SpecT<1> {
   using T = __half2;
   __device__ static __forceinline__ void cmac_conj(float2 &y, __half2 a, __half2 b) {
-    const float2 p = __half22float2(__hmul2(a, b));                        // (ax bx, ay by)
-    const float2 q = __half22float2(__hmul2(a, __lowhigh2highlow(b)));     // (ax by, ay bx)
-    y.x += p.x + p.y;
-    y.y += q.y - q.x;
+    asm("{\n .reg .b16 ax, ay, bx, by, nax;\n mov.b32 {ax, ay}, %2;\n mov.b32 {bx, by}, %3;\n neg.f16 nax, ax;\n"
+        " fma.rn.f32.f16 %0, ay, by, %0;\n fma.rn.f32.f16 %0, ax, bx, %0;\n"
+        " fma.rn.f32.f16 %1, nax, by, %1;\n fma.rn.f32.f16 %1, ay, bx, %1;\n}"
+        : "+f"(y.x), "+f"(y.y)
+        : "r"(*reinterpret_cast<const unsigned *>(&a)), "r"(*reinterpret_cast<const unsigned *>(&b)));
   }
   __device__ static __forceinline__ float2 f2(__half2 a) { return __half22float2(a); }
 };
 template <> struct SpecT<2> {
   using T = __nv_bfloat162;
   __device__ static __forceinline__ void cmac_conj(float2 &y, __nv_bfloat162 a, __nv_bfloat162 b) {
-    const float2 p = __bfloat1622float2(__hmul2(a, b));
-    const float2 q = __bfloat1622float2(__hmul2(a, __lowhigh2highlow(b)));
-    y.x += p.x + p.y;
-    y.y += q.y - q.x;
+    asm("{\n .reg .b16 ax, ay, bx, by, nax;\n mov.b32 {ax, ay}, %2;\n mov.b32 {bx, by}, %3;\n neg.bf16 nax, ax;\n"
+        " fma.rn.f32.bf16 %0, ay, by, %0;\n fma.rn.f32.bf16 %0, ax, bx, %0;\n"
+        " fma.rn.f32.bf16 %1, nax, by, %1;\n fma.rn.f32.bf16 %1, ay, bx, %1;\n}"
+        : "+f"(y.x), "+f"(y.y)
+        : "r"(*reinterpret_cast<const unsigned *>(&a)), "r"(*reinterpret_cast<const unsigned *>(&b)));
   }
   __device__ static __forceinline__ float2 f2(__nv_bfloat162 a) { return __bfloat1622float2(a); }
 };
