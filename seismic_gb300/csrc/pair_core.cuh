@@ -265,6 +265,77 @@ __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, 
   }
 }
 
+// The P = 4096 transform (radix 16 x 16 x 16, G = 128, two jobs a thread)
+// through a half-size exchange buffer of padded_len<2048>(): each of the two
+// exchanges runs in two rounds, round h moving the values whose index lies
+// in [2048 h, 2048 h + 2048) -- the first exchange's column set h (ca, then
+// cb), the second's job h -- and the readers taking r in [8 h, 8 h + 8) of
+// both jobs, at the same local index t + 128 q + 256 r' in both rounds.
+// Round h's reads land in the registers round h wrote (v[16 h .. 16 h + 15])
+// and a compile-time renaming puts them back in v[16 q + r] order.  Two more
+// group barriers per exchange buy half the shared memory, which the staged
+// form gives to its ring.  Same arithmetic as inverse_fft_group, bit for bit.
+__device__ __forceinline__ void split_exchange_read(const float2 *buf, float2 (&v)[32], int t, int h) {
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const float2 *row = buf + pad16(t + q * 128);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[16 * h + 8 * q + r] = row[r * 256 * 17 / 16];
+  }
+}
+// v[0..7] = job 0 r 0..7, v[8..15] = job 1 r 0..7, v[16..23] = job 0 r 8..15,
+// v[24..31] = job 1 r 8..15  ->  v[16 q + r]
+__device__ __forceinline__ void split_exchange_order(float2 (&v)[32]) {
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    const float2 x = v[8 + r];
+    v[8 + r] = v[16 + r];
+    v[16 + r] = x;
+  }
+}
+template <int P>
+__device__ __forceinline__ void inverse_fft_group_split(float2 (&v)[32], float2 *buf, int t, int g, int ca, int cb,
+                                                        const TwiddleRoots<P, 1> &roots, bool *stop = nullptr) {
+  static_assert(P == 4096 && FftPlan<P>::R2 == 16 && FftPlan<P>::R3 == 16 && FftPlan<P>::R4 == 0,
+                "inverse_fft_group_split: the P = 4096 plan");
+  constexpr int G = P / 32;
+  dft<16, 1>(&v[0]);
+  dft<16, 1>(&v[16]);
+  // first exchange: columns ca (indices < 2048), then cb (>= 2048)
+#pragma unroll
+  for (int r = 0; r < 16; ++r) buf[pad16(ca * 16 + r)] = v[r];
+  if (stop) {
+    *stop = group_sync_any<G>(g, *stop);
+    if (*stop) return;
+  } else {
+    group_sync<G>(g);
+  }
+  split_exchange_read(buf, v, t, 0);
+  group_sync<G>(g);
+#pragma unroll
+  for (int r = 0; r < 16; ++r) buf[pad16(cb * 16 + r - 2048)] = v[16 + r];
+  group_sync<G>(g);
+  split_exchange_read(buf, v, t, 1);
+  split_exchange_order(v);
+  group_sync<G>(g);
+  pass_compute_held<P, 16, 16, 1>(v, roots.template get<2>());
+  // second exchange: job h's sixteen values at (j / 16) 256 + j % 16 + 16 r
+  // with j = t + 128 h, local index (t / 16) 256 + t % 16 + 16 r
+  float2 *wrow = buf + pad16((t / 16) * 256 + t % 16);
+#pragma unroll
+  for (int r = 0; r < 16; ++r) wrow[r * 16 * 17 / 16] = v[r];
+  group_sync<G>(g);
+  split_exchange_read(buf, v, t, 0);
+  group_sync<G>(g);
+#pragma unroll
+  for (int r = 0; r < 16; ++r) wrow[r * 16 * 17 / 16] = v[16 + r];
+  group_sync<G>(g);
+  split_exchange_read(buf, v, t, 1);
+  split_exchange_order(v);
+  group_sync<G>(g);
+  pass_compute_held<P, 16, 256, 1>(v, roots.template get<3>());
+}
+
 // Bit q * RL + r set when the thread's last-pass value v[q * RL + r] (output
 // index last_pass_index) lies inside the lag window 1 - shift .. shift (every
 // bit for a window as wide as P).  It depends only on t and shift, so a

@@ -59,14 +59,20 @@ constexpr int kStagedRingMax = 16;
 constexpr int kItemRing = 16;
 constexpr size_t kStagedSmemBudget = 227 * 1024;
 
-template <int P, int NWARP, int RU> struct Staged {  // RU: chunks r per ring slot
+template <int P, int NWARP, int RU, int ST> struct Staged {  // RU: chunks r per ring slot, ST: spectra type
   static constexpr int G = P / 32;
   static constexpr int NG = NWARP * 32 / G;  // FFT groups per CTA
   static constexpr int S = P / 16;
   static constexpr int NW = (G + 31) / 32;
   static constexpr int CONSUMERS = NWARP * 32;  // FFT threads
   static constexpr int THREADS = CONSUMERS + 32;  // + the producer warp
-  static constexpr size_t EX_BYTES = (size_t)NG * padded_len<P>() * sizeof(float2);
+  // exchange buffer of one group.  P = 4096 with FP32 spectra runs its
+  // exchanges in two halves (inverse_fft_group_split) and leaves the other
+  // half to the ring: N=4096 C=3 94.6 -> 102.3 M pairs/s.  FP16 spectra,
+  // whose item nearly fits the ring already, measured 102.4 -> 92.2 with it.
+  static constexpr bool SPLIT_EX = P == 4096 && ST == 0;
+  static constexpr int EX_LEN = SPLIT_EX ? padded_len<P / 2>() : padded_len<P>();
+  static constexpr size_t EX_BYTES = (size_t)NG * EX_LEN * sizeof(float2);
   static constexpr size_t RED_BYTES = (size_t)NG * NW * 8 * sizeof(unsigned);
   static constexpr size_t PROD_OFF = (EX_BYTES + RED_BYTES + 15) / 16 * 16;
   // producer area: cursor (48 B), abort flag (+48), probe mbarrier (+56),
@@ -160,7 +166,7 @@ template <int P, int NWARP, int RU, int ST>
 __device__ __forceinline__ void staged_issue(const PairArgs &a, const StagedGeom &gm, const CUtensorMap *imap,
                                              const CUtensorMap *jmap, StagedCursor *cur, StagedItem *items,
                                              unsigned char *dst, uint64_t *full, uint32_t sub_bytes) {
-  using SH = Staged<P, NWARP, RU>;
+  using SH = Staged<P, NWARP, RU, ST>;
   using ST_T = typename SpecT<ST>::T;
   constexpr int S = SH::S;
   const uint32_t ibytes = (uint32_t)(gm.ti * S * sizeof(ST_T));
@@ -193,7 +199,7 @@ template <int P, int NWARP, int RU, int ST>
 __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
     staged_pair_kernel(const PairArgs a, const __grid_constant__ CUtensorMap jmap,
                        const __grid_constant__ CUtensorMap imap) {
-  using SH = Staged<P, NWARP, RU>;
+  using SH = Staged<P, NWARP, RU, ST>;
   using ST_T = typename SpecT<ST>::T;
   constexpr int G = SH::G, S = SH::S, NW = SH::NW;
   // per-item constants come from the kernel parameters (PairArgs::item_*),
@@ -273,7 +279,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
     // ---------------------------------------------------------- FFT groups
     const int g = threadIdx.x / G;
     const int t = threadIdx.x % G;
-    float2 *buf = bufs + g * padded_len<P>();
+    float2 *buf = bufs + g * SH::EX_LEN;
     unsigned *red = reds + g * NW * 8;
     TwiddleRoots<P, 1> roots;
     roots.load(t, a.twiddles);
@@ -337,7 +343,10 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
       if (live) {  // uniform over the group
         float2 v[32];
         assemble_couple(y, t, v);
-        inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots, &stop);
+        if constexpr (SH::SPLIT_EX)
+          inverse_fft_group_split<P>(v, buf, t, g, ca, cb, roots, &stop);
+        else
+          inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots, &stop);
         if (stop) break;
         scan_and_write<P, kLivenessVote<P, ST>>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist, wmask, buf);
       } else if (group_sync_any<G>(g, stop)) {
@@ -472,7 +481,7 @@ long long staged_items_total(int P, const PairArgs &a) {
 // buffers (and room for the largest shared histogram), in slots of RU chunks
 // of the item's TI + TJ rows; at most kStagedRingMax.
 template <int P, int NWARP, int RU, int ST> static int staged_ring_slots(const PairArgs &a, size_t *unit_bytes) {
-  using SH = Staged<P, NWARP, RU>;
+  using SH = Staged<P, NWARP, RU, ST>;
   const StagedGeom gm = staged_geom(SH::NG, staged_item_rows(SH::NG, a));
   const size_t unit = (size_t)RU * (gm.ti + gm.tj) * SH::S * sizeof(typename SpecT<ST>::T);
   if (unit_bytes) *unit_bytes = unit;
@@ -483,7 +492,7 @@ template <int P, int NWARP, int RU, int ST> static int staged_ring_slots(const P
 
 template <int P, int NWARP, int RU, int ST>
 static cudaError_t launch_staged_t(const PairArgs &a0, int sm_count, cudaStream_t s) {
-  using SH = Staged<P, NWARP, RU>;
+  using SH = Staged<P, NWARP, RU, ST>;
   using ST_T = typename SpecT<ST>::T;
   PairArgs a = a0;
   a.item_i = staged_item_rows(SH::NG, a);
