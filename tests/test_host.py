@@ -4,6 +4,7 @@ drop-in's padding, and the pair scheduler's coverage of the triangle."""
 import ctypes
 import importlib.util
 import os
+import math
 import subprocess
 
 import numpy as np
@@ -167,9 +168,9 @@ def test_scheduler_covers_triangle_exactly_once(n, tile, band):
 
 
 def _staged_pairs(n, t, band, begin=0, end=None):
-    """Pairs written by items [begin, end) of the staged form (pairs_staged.cu):
-    item w is tile w // t in band order and its row w % t; group g takes
-    j0 + 2g and j0 + 2g + 1, t = 2 * groups."""
+    """Pairs written by items [begin, end) of the staged form with one i per
+    item (TI = 1 in pairs_staged.cu): item w is tile w // t in band order and
+    its row w % t; group g takes j0 + 2g and j0 + 2g + 1, t = 2 * groups."""
     nb = (n + t - 1) // t
     end = t * nb * (nb + 1) // 2 if end is None else end
     seen = []
@@ -187,6 +188,83 @@ def _staged_pairs(n, t, band, begin=0, end=None):
 def test_staged_scheduler_covers_triangle_exactly_once(n, t, band):
     seen = _staged_pairs(n, t, band)
     assert len(seen) == len(set(seen)) == n * (n + 1) // 2
+
+
+def _staged_geom(ng, ti):
+    """Item geometry of the staged form (pairs_staged.cu staged_geom): TI i
+    events x TJ = 2 ng / TI j events, square tiles of TS = lcm(TI, TJ)."""
+    tj = 2 * ng // ti
+    ts = ti // math.gcd(ti, tj) * tj
+    jpt = ts // tj
+    return ti, tj, ts, jpt, (ts // ti) * jpt
+
+
+def _staged_geom_pairs(n, ng, ti, band, begin=0, end=None):
+    """Pairs written by items [begin, end) of the triangle (staged_decode):
+    item w is tile w // ipt in band order, item k = w % ipt at tile row
+    k // jpt and column k % jpt; group g takes i0 + g // (TJ/2) and the
+    couple j0 + 2 (g % (TJ/2)), +1."""
+    ti, tj, ts, jpt, ipt = _staged_geom(ng, ti)
+    nb = (n + ts - 1) // ts
+    end = ipt * nb * (nb + 1) // 2 if end is None else end
+    seen = []
+    for w in range(begin, end):
+        x, k = divmod(w, ipt)
+        bi, bj = _band_tile(x, nb, band)
+        i0, j0 = bi * ts + (k // jpt) * ti, bj * ts + (k % jpt) * tj
+        for g in range(ng):
+            gi, gc = divmod(g, tj // 2)
+            for j in (j0 + 2 * gc, j0 + 2 * gc + 1):
+                if i0 + gi < n and j < n and j >= i0 + gi:
+                    seen.append((i0 + gi, j))
+    return seen
+
+
+@pytest.mark.parametrize("n,ng,ti,band", [(1, 24, 6, 0), (7, 24, 6, 0), (203, 24, 6, 2), (203, 30, 6, 3),
+                                          (100, 15, 5, 1), (61, 3, 3, 4), (90, 7, 7, 2), (50, 6, 3, 0),
+                                          (77, 12, 4, 5), (33, 24, 1, 2), (45, 12, 12, 1)])
+def test_staged_items_cover_triangle_exactly_once(n, ng, ti, band):
+    """TI x TJ work items (any TI dividing the group count) write every pair
+    of the triangle once, and the items of row band k (band_first_tile(k) x
+    items per tile onwards) write exactly the band's packed rows, which the
+    host entry point copies back chunk by chunk."""
+    seen = _staged_geom_pairs(n, ng, ti, band)
+    assert len(seen) == len(set(seen)) == n * (n + 1) // 2
+    _, _, ts, _, ipt = _staged_geom(ng, ti)
+    nb = (n + ts - 1) // ts
+    b = band if 0 < band <= nb else nb
+    for k in range((nb + b - 1) // b):
+        r0, r1 = min(k * b, nb), min((k + 1) * b, nb)
+        first = lambda r: r * nb - r * (r - 1) // 2
+        rows = {i for i, _ in _staged_geom_pairs(n, ng, ti, band, first(r0) * ipt, first(r1) * ipt)}
+        assert rows == set(range(r0 * ts, min(r1 * ts, n)))
+
+
+@pytest.mark.parametrize("nq,ncols,ng,ti", [(1, 50, 24, 1), (7, 113, 24, 2), (7, 113, 24, 3), (64, 200, 15, 5),
+                                            (5, 9, 6, 3), (13, 31, 30, 6)])
+def test_staged_rect_items_cover_rectangle_exactly_once(nq, ncols, ng, ti):
+    """Rectangle items: column block w // ceil(nq / TI) of TJ catalog events,
+    query block w % that of TI queries (queries past the last are idle)."""
+    ti, tj, _, _, _ = _staged_geom(ng, ti)
+    nqb = (nq + ti - 1) // ti
+    seen = []
+    for w in range(nqb * ((ncols + tj - 1) // tj)):
+        blk, qb = divmod(w, nqb)
+        for g in range(ng):
+            gi, gc = divmod(g, tj // 2)
+            i, ja = qb * ti + gi, blk * tj + 2 * gc
+            if i < nq and ja < ncols:
+                seen.append((i, ja))
+                if ja + 1 < ncols:
+                    seen.append((i, ja + 1))
+    assert len(seen) == len(set(seen)) == nq * ncols
+
+
+def test_staged_item_row_division():
+    """A group's item row g // (TJ/2) as (g * ceil(2^16 / (TJ/2))) >> 16."""
+    for d in range(1, 65):
+        m = (65536 + d - 1) // d
+        assert all((g * m) >> 16 == g // d for g in range(64))
 
 
 def test_native_api_rejects_bad_sizes_without_gpu(built_lib):
