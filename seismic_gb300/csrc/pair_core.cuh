@@ -265,43 +265,76 @@ __device__ __forceinline__ void inverse_fft_group(float2 (&v)[32], float2 *buf, 
   }
 }
 
-// The P = 4096 transform (radix 16 x 16 x 16, G = 128, two jobs a thread)
-// through a half-size exchange buffer of padded_len<2048>(): each of the two
-// exchanges runs in two rounds, round h moving the values whose index lies
-// in [2048 h, 2048 h + 2048) -- the first exchange's column set h (ca, then
-// cb), the second's job h -- and the readers taking r in [8 h, 8 h + 8) of
-// both jobs, at the same local index t + 128 q + 256 r' in both rounds.
-// Round h's reads land in the registers round h wrote (v[16 h .. 16 h + 15])
-// and a compile-time renaming puts them back in v[16 q + r] order.  Two more
-// group barriers per exchange buy half the shared memory, which the staged
-// form gives to its ring.  Same arithmetic as inverse_fft_group, bit for bit.
-__device__ __forceinline__ void split_exchange_read(const float2 *buf, float2 (&v)[32], int t, int h) {
+// inverse_fft_group through a half-size exchange buffer of padded_len<P/2>():
+// each exchange runs in two rounds, round h moving the values whose index
+// lies in [h P/2, (h+1) P/2).  Readers of a radix-R pass take r in
+// [h R/2, (h+1) R/2) of every job: index t + q G + r P/R, with t + q G < P/R,
+// lies in round h's half exactly then, at the same local index t + q G +
+// r' P/R in both rounds.  Writers: after pass 1 the column set h (ca, then
+// cb: ca < S/2 <= cb); after a later pass of radix R and stride NS the jobs
+// q in [h J/2, (h+1) J/2), whose indices (j / NS) NS R + j % NS + r NS lie in
+// half h when P / (2R) is a multiple of NS.  Round h's reads land in the
+// registers round h wrote (v[16 h .. 16 h + 15]) and a compile-time renaming
+// restores the v[q R + r] order.  Two more group barriers per exchange buy
+// half the shared memory, which the staged form gives to its ring.  Same
+// arithmetic as inverse_fft_group, bit for bit.
+template <int P, int R> __device__ __forceinline__ void split_read(const float2 *buf, float2 (&v)[32], int t, int h) {
+  constexpr int G = P / 32, J = 32 / R;
 #pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    const float2 *row = buf + pad16(t + q * 128);
+  for (int q = 0; q < J; ++q) {
+    const float2 *row = buf + pad16(t + q * G);
 #pragma unroll
-    for (int r = 0; r < 8; ++r) v[16 * h + 8 * q + r] = row[r * 256 * 17 / 16];
+    for (int r = 0; r < R / 2; ++r) v[16 * h + (R / 2) * q + r] = row[r * (P / R) * 17 / 16];
   }
 }
-// v[0..7] = job 0 r 0..7, v[8..15] = job 1 r 0..7, v[16..23] = job 0 r 8..15,
-// v[24..31] = job 1 r 8..15  ->  v[16 q + r]
-__device__ __forceinline__ void split_exchange_order(float2 (&v)[32]) {
+// v[16 h + (R/2) q + r'] holds job q's value r = h R/2 + r'  ->  v[q R + r]
+template <int R> __device__ __forceinline__ void split_order(float2 (&v)[32]) {
+  constexpr int J = 32 / R;
+  float2 w[32];
 #pragma unroll
-  for (int r = 0; r < 8; ++r) {
-    const float2 x = v[8 + r];
-    v[8 + r] = v[16 + r];
-    v[16 + r] = x;
+  for (int h = 0; h < 2; ++h)
+#pragma unroll
+    for (int q = 0; q < J; ++q)
+#pragma unroll
+      for (int r = 0; r < R / 2; ++r) w[q * R + h * (R / 2) + r] = v[16 * h + (R / 2) * q + r];
+#pragma unroll
+  for (int e = 0; e < 32; ++e) v[e] = w[e];
+}
+template <int P, int R, int NS>
+__device__ __forceinline__ void split_write(float2 *buf, const float2 (&v)[32], int t, int h) {
+  constexpr int G = P / 32, J = 32 / R;
+  static_assert(NS % 16 == 0 && (P / (2 * R)) % NS == 0 && J % 2 == 0, "split_write: jobs not split by halves");
+#pragma unroll
+  for (int q = h * (J / 2); q < (h + 1) * (J / 2); ++q) {
+    const int j = t + q * G;
+    float2 *row = buf + pad16((j / NS) * NS * R + (j % NS) - h * (P / 2));
+#pragma unroll
+    for (int r = 0; r < R; ++r) row[r * NS * 17 / 16] = v[q * R + r];
   }
+}
+// One later exchange (writer: radix RW, stride NSW; reader: radix RR) in two
+// rounds; the first barrier is a plain one (the abort vote sits at pass 1's).
+template <int P, int RW, int NSW, int RR>
+__device__ __forceinline__ void split_exchange(float2 *buf, float2 (&v)[32], int t, int g) {
+  constexpr int G = P / 32;
+  split_write<P, RW, NSW>(buf, v, t, 0);
+  group_sync<G>(g);
+  split_read<P, RR>(buf, v, t, 0);
+  group_sync<G>(g);
+  split_write<P, RW, NSW>(buf, v, t, 1);
+  group_sync<G>(g);
+  split_read<P, RR>(buf, v, t, 1);
+  split_order<RR>(v);
+  group_sync<G>(g);
 }
 template <int P>
 __device__ __forceinline__ void inverse_fft_group_split(float2 (&v)[32], float2 *buf, int t, int g, int ca, int cb,
                                                         const TwiddleRoots<P, 1> &roots, bool *stop = nullptr) {
-  static_assert(P == 4096 && FftPlan<P>::R2 == 16 && FftPlan<P>::R3 == 16 && FftPlan<P>::R4 == 0,
-                "inverse_fft_group_split: the P = 4096 plan");
+  using PL = FftPlan<P>;
   constexpr int G = P / 32;
   dft<16, 1>(&v[0]);
   dft<16, 1>(&v[16]);
-  // first exchange: columns ca (indices < 2048), then cb (>= 2048)
+  // first exchange: columns ca (indices < P/2), then cb (>= P/2)
 #pragma unroll
   for (int r = 0; r < 16; ++r) buf[pad16(ca * 16 + r)] = v[r];
   if (stop) {
@@ -310,30 +343,23 @@ __device__ __forceinline__ void inverse_fft_group_split(float2 (&v)[32], float2 
   } else {
     group_sync<G>(g);
   }
-  split_exchange_read(buf, v, t, 0);
+  split_read<P, PL::R2>(buf, v, t, 0);
   group_sync<G>(g);
 #pragma unroll
-  for (int r = 0; r < 16; ++r) buf[pad16(cb * 16 + r - 2048)] = v[16 + r];
+  for (int r = 0; r < 16; ++r) buf[pad16(cb * 16 + r - P / 2)] = v[16 + r];
   group_sync<G>(g);
-  split_exchange_read(buf, v, t, 1);
-  split_exchange_order(v);
+  split_read<P, PL::R2>(buf, v, t, 1);
+  split_order<PL::R2>(v);
   group_sync<G>(g);
-  pass_compute_held<P, 16, 16, 1>(v, roots.template get<2>());
-  // second exchange: job h's sixteen values at (j / 16) 256 + j % 16 + 16 r
-  // with j = t + 128 h, local index (t / 16) 256 + t % 16 + 16 r
-  float2 *wrow = buf + pad16((t / 16) * 256 + t % 16);
-#pragma unroll
-  for (int r = 0; r < 16; ++r) wrow[r * 16 * 17 / 16] = v[r];
-  group_sync<G>(g);
-  split_exchange_read(buf, v, t, 0);
-  group_sync<G>(g);
-#pragma unroll
-  for (int r = 0; r < 16; ++r) wrow[r * 16 * 17 / 16] = v[16 + r];
-  group_sync<G>(g);
-  split_exchange_read(buf, v, t, 1);
-  split_exchange_order(v);
-  group_sync<G>(g);
-  pass_compute_held<P, 16, 256, 1>(v, roots.template get<3>());
+  pass_compute_held<P, PL::R2, 16, 1>(v, roots.template get<2>());
+  if constexpr (PL::R3 != 0) {
+    split_exchange<P, PL::R2, 16, PL::R3>(buf, v, t, g);
+    pass_compute_held<P, PL::R3, 16 * PL::R2, 1>(v, roots.template get<3>());
+    if constexpr (PL::R4 != 0) {
+      split_exchange<P, PL::R3, 16 * PL::R2, PL::R4>(buf, v, t, g);
+      pass_compute_held<P, PL::R4, 16 * PL::R2 * PL::R3, 1>(v, roots.template get<4>());
+    }
+  }
 }
 
 // Bit q * RL + r set when the thread's last-pass value v[q * RL + r] (output

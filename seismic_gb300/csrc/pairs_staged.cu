@@ -68,8 +68,12 @@ template <int P, int NWARP, int RU, int ST> struct Staged {  // RU: chunks r per
   static constexpr int THREADS = CONSUMERS + 32;  // + the producer warp
   // exchange buffer of one group.  P = 4096 with FP32 spectra runs its
   // exchanges in two halves (inverse_fft_group_split) and leaves the other
-  // half to the ring: N=4096 C=3 94.6 -> 102.3 M pairs/s.  FP16 spectra,
-  // whose item nearly fits the ring already, measured 102.4 -> 92.2 with it.
+  // half to the ring: N=4096 C=3 94.6 -> 102.3 M pairs/s.  Elsewhere the
+  // extra barriers cost more than the ring gains (measured, M pairs/s,
+  // full / split exchange): FP16 spectra at that shape 102.5 / 92.0; the
+  // overlap-save Q=512 x 4 form 831 / 813; Q=1024 x 2 with three channels
+  // 340 / 336; plain P=2048 one channel 268 / 262 -- only plain P=2048 with
+  // three channels gained (198 / 211).
   static constexpr bool SPLIT_EX = P == 4096 && ST == 0;
   static constexpr int EX_LEN = SPLIT_EX ? padded_len<P / 2>() : padded_len<P>();
   static constexpr size_t EX_BYTES = (size_t)NG * EX_LEN * sizeof(float2);
