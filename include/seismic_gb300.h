@@ -213,8 +213,10 @@ int seismic_pairs_device_range(const void *d_spectra, const double *d_norms, lon
                                int padded_size, int prescaled, int shift, float threshold, int n_classes_hist,
                                long long couple_begin, long long couple_end, float *d_vals_pos, int *d_lags_pos,
                                float *d_vals_neg, int *d_lags_neg, int *d_max_hist, int *d_min_hist, void *stream);
-/* Number of work items ("couples", two pairs each) of the triangle of
- * n_events at this padded size and channel count. */
+/* Number of work items of the pair kernel on the triangle of n_events at
+ * this padded size and channel count: couples (two pairs each) in the
+ * direct-load form, blocks of TI x TJ events in the staged form (the name
+ * keeps the first meaning).  Only ranges of this count are meaningful. */
 long long seismic_pair_couples(long long n_events, int padded_size, int n_channels);
 
 /* seismic_xcorr_device for callers that cannot allocate device memory.
