@@ -143,6 +143,44 @@ def test_large_padded_sizes_native(cuda_ok):
     assert lib.seismic_xcorr_workspace_bytes(4, 1, 20000, 3000, 32768, 0) == 0
 
 
+@pytest.mark.parametrize("n,c,length,shift", [
+    (11, 3, 700, 300),    # P = 1024, three channels: the lane vote
+    (9, 40, 400, 200),    # P = 1024, forty channels: lanes 0..31 vote, thread 0 checks the rest
+    (8, 3, 2048, 1500),   # P = 4096, the split exchange
+])
+def test_multichannel_zero_norms(cuda_ok, monkeypatch, n, c, length, shift):
+    """Multichannel (prescaled) pairs with zero-norm channels: a pair is live
+    when some channel has both norms nonzero, zero channels add nothing to the
+    mean, an all-zero event gives zeros.  Against FP64, and the staged form
+    bit-identical to the direct form."""
+    import torch
+    ev = synth.family_catalog(n, c, length, n_families=2, seed=n + c)
+    ev[2, 1] = 0.0            # one channel of event 2
+    ev[5] = 0.0               # all of event 5
+    ev[6, :c - 1] = 0.0       # event 6 keeps only its last channel
+    ev[7, c - 1] = 0.0        # event 7 lacks exactly that one: (6, 7) has no common channel
+    t = torch.from_numpy(ev).cuda()
+    i, j = O.triu_pairs(n)
+    ref = O.fp64_xcorr(ev, shift, i, j, padded=xcorr.resolve_padded_size(length, shift))
+    got = {}
+    for kind in ("staged", "direct"):
+        monkeypatch.setenv("SEISMIC_PAIR_KERNEL", kind)
+        r = xcorr.xcorr(t, shift, threshold=0.0, n_classes_hist=8)
+        torch.cuda.synchronize()
+        got[kind] = [x.cpu().numpy() for x in (r.vals_pos, r.lags_pos, r.vals_neg, r.lags_neg)] + \
+                    [r.max_hist.cpu().numpy(), r.min_hist.cpu().numpy()]
+        ag = O.agreement(*got[kind][:4], ref)
+        assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, (kind, ag)
+        assert ag.lag_mismatch == 0, (kind, ag)
+        for e in range(n):  # the all-zero event: zeros everywhere
+            k = xcorr.packed_index(np.array([min(e, 5)]), np.array([max(e, 5)]), n)[0]
+            assert got[kind][0][k] == 0 and got[kind][2][k] == 0 and got[kind][1][k] == 0
+        k = xcorr.packed_index(np.array([6]), np.array([7]), n)[0]
+        assert got[kind][0][k] == 0 and got[kind][2][k] == 0  # no channel in common
+    for a, b in zip(got["staged"], got["direct"]):
+        np.testing.assert_array_equal(a, b)
+
+
 def test_zero_norm_event_defined(cuda_ok):
     ev = synth.ricker_catalog(6, 256, seed=31)[:, 0].copy()
     ev[3] = 0.0
