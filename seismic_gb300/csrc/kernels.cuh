@@ -195,7 +195,8 @@ __host__ __device__ __forceinline__ long long band_first_tile(long long k, long 
 }
 
 // ---- staged pair form (pairs_staged.cu): spectra staged into shared memory
-// by TMA (P = 4096 by default).  Work items are (event i, T consecutive j).
+// by TMA (P = 512 .. 4096).  Work items are TI events i x TJ consecutive j
+// (pairs_staged.cu, StagedGeom).
 bool staged_supported(int P, const PairArgs &a);
 // The staged form can run at all (not disabled by SEISMIC_PAIR_KERNEL=direct,
 // and the driver's tensor-map encoder is available).
