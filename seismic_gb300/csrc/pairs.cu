@@ -157,7 +157,7 @@ __device__ __forceinline__ void pair_body(const PairArgs &a, long long w_first, 
     float2 v[32];
     assemble_couple(y, t, v);
     inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots);
-    scan_and_write<P, kLivenessVote<P, ST>>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist, wmask, buf);
+    scan_and_write<P, kLivenessVote<P, ST>, kScanRowSkip<P, ST>>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist, wmask, buf);
   }
 }
 

@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(NWARP * 32 + 32, 1)
         else
           inverse_fft_group<P>(v, buf, t, g, ca, cb, a.twiddles, roots, &stop);
         if (stop) break;
-        scan_and_write<P, kLivenessVote<P, ST>>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist, wmask, buf);
+        scan_and_write<P, kLivenessVote<P, ST>, kScanRowSkip<P, ST>>(a, v, i, ja, i, jb, out_b, t, g, red, hist, smem_hist, wmask, buf);
       } else if (group_sync_any<G>(g, stop)) {
         break;
       }
