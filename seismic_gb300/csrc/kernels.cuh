@@ -115,7 +115,7 @@ struct PairArgs {
   long long n_query;
   long long col_begin;
   long long n_cols;
-  // Staged form (pairs_staged.cu) only: tile columns per L2 band of the
+  // Staged form (staged_core.cuh) only: tile columns per L2 band of the
   // triangle walk, the shared-memory ring depth, and the device error flag
   // set when a bounded wait runs out.
   int band_tiles;
@@ -194,9 +194,9 @@ __host__ __device__ __forceinline__ long long band_first_tile(long long k, long 
   return r0 * nb - r0 * (r0 - 1) / 2;
 }
 
-// ---- staged pair form (pairs_staged.cu): spectra staged into shared memory
+// ---- staged pair form (staged_core.cuh): spectra staged into shared memory
 // by TMA (P = 512 .. 4096).  Work items are TI events i x TJ consecutive j
-// (pairs_staged.cu, StagedGeom).
+// (staged_core.cuh, StagedGeom).
 bool staged_supported(int P, const PairArgs &a);
 // The staged form can run at all (not disabled by SEISMIC_PAIR_KERNEL=direct,
 // and the driver's tensor-map encoder is available).

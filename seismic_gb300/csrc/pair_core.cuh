@@ -1,4 +1,4 @@
-// Device building blocks of the pair kernels (pairs.cu, pairs_staged.cu):
+// Device building blocks of the pair kernels (pairs.cu, staged_core.cuh):
 // the conj-product accumulation of one couple, the assembly of its complex
 // spectrum, the group inverse FFT, the lag-window scan with first-occurrence
 // argmax / argmin, and the normalise / histogram / threshold / packed-write

@@ -1,5 +1,5 @@
 // Kernels (b) + (c): fused pair-tile correlation with an upper-triangle tile
-// scheduler (direct-load form; pairs_staged.cu holds the TMA-staged form).
+// scheduler (direct-load form; staged_core.cuh holds the TMA-staged form).
 //
 // Replaces, per pair (i, j >= i) of the packed upper triangle:
 //   ElementWiseMultiplication  Correlation_in_OMP/correlation_c.cpp:188-193
@@ -16,7 +16,7 @@
 // are dealt to groups of G = P/32 threads round-robin, the groups of one CTA
 // taking neighbouring couples of the same tile, whose spectra they read
 // straight from global memory (L2).  This form serves every size P and the
-// batched launch; pairs_staged.cu stages the spectra through shared memory.
+// batched launch; staged_core.cuh stages the spectra through shared memory.
 #include <algorithm>
 #include "pair_core.cuh"
 

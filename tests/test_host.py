@@ -169,7 +169,7 @@ def test_scheduler_covers_triangle_exactly_once(n, tile, band):
 
 def _staged_pairs(n, t, band, begin=0, end=None):
     """Pairs written by items [begin, end) of the staged form with one i per
-    item (TI = 1 in pairs_staged.cu): item w is tile w // t in band order and
+    item (TI = 1 in staged_core.cuh): item w is tile w // t in band order and
     its row w % t; group g takes j0 + 2g and j0 + 2g + 1, t = 2 * groups."""
     nb = (n + t - 1) // t
     end = t * nb * (nb + 1) // 2 if end is None else end
@@ -191,7 +191,7 @@ def test_staged_scheduler_covers_triangle_exactly_once(n, t, band):
 
 
 def _staged_geom(ng, ti):
-    """Item geometry of the staged form (pairs_staged.cu staged_geom): TI i
+    """Item geometry of the staged form (staged_core.cuh staged_geom): TI i
     events x TJ = 2 ng / TI j events, square tiles of TS = lcm(TI, TJ)."""
     tj = 2 * ng // ti
     ts = ti // math.gcd(ti, tj) * tj
