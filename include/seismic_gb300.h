@@ -29,7 +29,10 @@
  *    row-major at index i*N - i*(i-1)/2 + (j-i) (:269), 64-bit;
  *  - lags d = 1-shift .. shift, series value at lag d = sum_k x_i[k] x_j[k-d]
  *    (circular of size paddedSize), first strict maximum above 0 / minimum
- *    below 0 in increasing d, else value 0 and lag 0 (:102-111);
+ *    below 0 in increasing d, else value 0 and lag 0 (:102-111).  A
+ *    paddedSize that is not a power of two is accepted where it holds the
+ *    lag window (paddedSize >= event_length + shift: the circular series is
+ *    then the linear one, computed at the next power of two);
  *  - coefficient = peak / (paddedSize * |x_i| * |x_j|), norms in FP64
  *    (:115,:127); with C > 1 channels, the mean over channels of the
  *    per-channel normalised series;

@@ -230,9 +230,11 @@ static int validate(long long n_events, int n_channels, int event_length, int pa
   if (is_lag_form(form) ? (padded < kMinP || padded > kMaxPadded || (padded & (padded - 1)) != 0)
                         : !fft_size_ok(padded, event_length, shift, n_channels, form, plain_only))
     return set_status(SEISMIC_ERR_UNSUPPORTED_SIZE,
-                      plain_only ? "paddedSize %d unsupported (power of two in [64, 16384])"
-                                 : "paddedSize %d unsupported (power of two in [64, 16384]; larger ones where the "
-                                   "overlap-save form takes the lag window: shift <= 1792, FP32 or FP16 spectra)",
+                      plain_only ? "paddedSize %d unsupported (power of two in [64, 16384], or any size >= "
+                                   "event_length + shift up to 16384)"
+                                 : "paddedSize %d unsupported (power of two in [64, 16384], or any size >= "
+                                   "event_length + shift; larger ones where the overlap-save form takes the lag "
+                                   "window: shift <= 1792, FP32 or FP16 spectra)",
                       padded);
   if (event_length > padded)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "event_length %d exceeds paddedSize %d", event_length, padded);
@@ -543,6 +545,7 @@ size_t seismic_xcorr_workspace_bytes(long long n_events, int n_channels, int eve
     return lag_workspace_bytes(n_events, n_channels, event_length, lag_planes(form));
   }
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  padded_size = effective_padded(padded_size, event_length, shift);
   if (!fft_size_ok(padded_size, event_length, shift, n_channels, form, false)) return 0;
   return fft_job(n_events, n_channels, event_length, shift, padded_size, form_stype(form)).total();
 }
@@ -551,6 +554,7 @@ int seismic_fft_plan(int event_length, int shift, int padded_size, int n_channel
                      int *blocks, int *block_length) {
   set_status(SEISMIC_OK, "");
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  padded_size = effective_padded(padded_size, event_length, shift);
   int s = validate(1, n_channels, event_length, padded_size, shift, 0, form);
   if (s) return s;
   if (is_lag_form(form)) return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "lag-GEMM forms use no transform");
@@ -599,6 +603,7 @@ int seismic_xcorr_device_stages(const float *d_events, long long n_events, int n
   if (stages != 3 && !workspace)
     return set_status(SEISMIC_ERR_INVALID_ARGUMENT, "running one stage needs the caller's workspace");
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  padded_size = effective_padded(padded_size, event_length, shift);
   int s = validate(n_events, n_channels, event_length, padded_size, shift, n_classes_hist, form);
   if (s) return s;
   if (!d_events || !d_vals_pos || !d_lags_pos || !d_vals_neg || !d_lags_neg)
@@ -703,6 +708,7 @@ int seismic_xcorr_host(const float *events, long long n_events, int n_channels, 
                        float *vals_neg, int *lags_neg, int *max_hist, int *min_hist) {
   set_status(SEISMIC_OK, "");
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  padded_size = effective_padded(padded_size, event_length, shift);
   int s = validate(n_events, n_channels, event_length, padded_size, shift, n_classes_hist, form);
   if (s) return s;
   if (!events || !vals_pos || !lags_pos || !vals_neg || !lags_neg)

@@ -14,6 +14,20 @@ constexpr int kMaxBatchP = 8192;          // batched launches (256-thread CTAs)
 constexpr int kMaxPadded = 1 << 24;       // beyond kMaxP: the overlap-save form only
 constexpr int kMaxBlockShift = 7 * 4096 / 16;  // its widest lag window: frames of Q = 4096, blocks >= Q / 8
 
+// A padded size that is not a power of two but holds the whole lag window
+// (padded >= event_length + shift) gives the reference's size-padded
+// circular correlation without aliasing, i.e. the linear correlation, which
+// any larger transform gives too: such a size runs at the next power of
+// two.  Others come back unchanged (an aliasing non-power-of-two size stays
+// unsupported).
+inline int effective_padded(int padded, int event_length, int shift) {
+  if (padded <= 0 || (padded & (padded - 1)) == 0) return padded;
+  if ((long long)event_length + shift > padded) return padded;
+  long long p = kMinP;
+  while (p < padded) p <<= 1;
+  return p <= kMaxPadded ? (int)p : padded;
+}
+
 // Layout of the packed half spectrum of one (event, channel) row:
 //   slot 0      = (Re X[0], Re X[P/2])   (both bins are real for real input)
 //   slot k>0    = X[k],  k = 1 .. P/2-1

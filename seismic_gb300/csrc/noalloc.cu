@@ -102,6 +102,7 @@ extern "C" int seismic_xcorr_device_noalloc(const float *d_events, long long n_e
                                             int *d_lags_neg, int *d_max_hist, int *d_min_hist, void *stream) {
   report_status(SEISMIC_OK, "");
   if (padded_size == 0) padded_size = seismic_resolve_padded_size(event_length, shift);
+  padded_size = effective_padded(padded_size, event_length, shift);
   int s = check_xcorr_args(n_events, n_channels, event_length, padded_size, shift, n_classes_hist,
                            SEISMIC_FORM_FP32, true);
   if (s) return s;

@@ -117,6 +117,31 @@ def test_sizes_vs_port(cuda_ok, n, length, shift, thr, nh):
     check_hist(got[4], got[5], exp.max_hist, exp.min_hist, r, nh)
 
 
+def test_non_power_of_two_padded_size_dropin(cuda_ok):
+    """The reference's C entry point with a paddedSize that is not a power of
+    two but holds the lag window: the size-3000 circular correlation the
+    reference computes is the linear one, against FP64 at that size."""
+    n, length, shift, padded = 23, 1000, 900, 3000
+    ev = synth.family_catalog(n, 1, length, n_families=3, seed=41)[:, 0]
+    lay = np.zeros((n, padded), np.float32)  # the reference's padded layout, rows of paddedSize
+    lay[:, :length] = ev
+    m = n * (n + 1) // 2
+    got = [np.zeros(m, np.float32), np.zeros(m, np.int32), np.zeros(m, np.float32), np.zeros(m, np.int32)]
+    hmax, hmin = np.zeros(10, np.int32), np.zeros(10, np.int32)
+    lib = _lib.lib()
+    fp, ip = _lib.c_float_p, _lib.c_int_p
+    lib.correlationCPP(lay.ctypes.data_as(fp), lay.ctypes.data_as(fp), n, length, shift, padded, 2, 1, 0.0, 10,
+                       got[0].ctypes.data_as(fp), got[1].ctypes.data_as(ip), got[2].ctypes.data_as(fp),
+                       got[3].ctypes.data_as(ip), hmax.ctypes.data_as(ip), hmin.ctypes.data_as(ip))
+    _lib.check(lib.seismic_last_error())
+    assert int(hmax.sum()) == m
+    i, j = O.triu_pairs(n)
+    ref = O.fp64_xcorr(ev, shift, i, j, padded=3000)
+    ag = O.agreement(*got[:4], ref)
+    assert ag.max_err_pos < 1e-5 and ag.max_err_neg < 1e-5, ag
+    assert ag.lag_mismatch == 0, ag
+
+
 def test_large_padded_sizes_native(cuda_ok):
     """The native entry point on long events: P = 16384 (plain, three channels)
     and a 2^17 padded size with a short lag window (overlap-save frames), each

@@ -267,6 +267,16 @@ def test_staged_item_row_division():
         assert all((g * m) >> 16 == g // d for g in range(64))
 
 
+def test_non_power_of_two_padded_sizes(built_lib):
+    """A padded size that is not a power of two but holds the lag window
+    (the circular series is then the linear one) gets the workspace of the
+    next power of two; an aliasing one is refused."""
+    ws = built_lib.seismic_xcorr_workspace_bytes
+    assert ws(8, 1, 1000, 1000, 3000, 0) == ws(8, 1, 1000, 1000, 4096, 0) > 0
+    assert ws(8, 1, 1000, 1000, 1999, 0) == 0       # 1000 + 1000 > 1999: aliasing
+    assert ws(8, 3, 700, 300, 1000, 0) == ws(8, 3, 700, 300, 1024, 0) > 0
+
+
 def test_native_api_rejects_bad_sizes_without_gpu(built_lib):
     """Argument validation runs before any CUDA call."""
     st = built_lib.seismic_xcorr_host(ctypes.c_void_p(1), 4, 1, 100, 100, 100, 96, 10, 0.0, 0, 0,
